@@ -1,0 +1,192 @@
+// Batched renders: many requests in one launch of the persistent kernel,
+// replayed from a CUDA graph (staging copy of the descriptors, queue-head
+// reset, kernel). Replaces the reference's one-render-per-cube loop
+// (src/main.cpp:242-264).
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "batch.h"
+
+using namespace birp;
+
+#define CKB(x)                                                                                 \
+  do {                                                                                         \
+    cudaError_t e_ = (x);                                                                      \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail(e_ == cudaErrorMemoryAllocation ? BIRP_ERR_NOMEM : BIRP_ERR_CUDA, "%s: %s", #x, \
+                  cudaGetErrorString(e_));                                                     \
+  } while (0)
+
+namespace birp {
+
+static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+static void free_batch(birp_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->h_stage) cudaFreeHost(b->h_stage);
+  if (b->h_out) cudaFreeHost(b->h_out);
+  if (b->d_stage) cudaFree(b->d_stage);
+  if (b->d_out) cudaFree(b->d_out);
+  if (b->d_counter) cudaFree(b->d_counter);
+  for (cudaEvent_t e : {b->e_start, b->e_kernel, b->e_end})
+    if (e) cudaEventDestroy(e);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out) {
+  if (birp_status s = check_init()) return s;
+  if (!out || max_requests < 1 || max_pixels < 1 || max_requests > (1 << 20))
+    return fail(BIRP_ERR_INVALID, "bad batch limits");
+  *out = nullptr;
+  birp_batch* b = new birp_batch();
+  b->max_req = max_requests;
+  b->max_px = max_pixels;
+  // staging block: hdr[4] | first[max+1] | order[max] | (16B aligned) RequestDev[max]
+  b->off_first = 4 * sizeof(int);
+  b->off_order = b->off_first + (size_t)(max_requests + 1) * sizeof(int);
+  b->off_reqs = align_up(b->off_order + (size_t)max_requests * sizeof(int), 16);
+  b->stage_bytes = b->off_reqs + (size_t)max_requests * sizeof(RequestDev);
+  auto bail = [&](birp_status s) {
+    free_batch(b);
+    return s;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaHostAlloc(&b->h_stage, b->stage_bytes, cudaHostAllocDefault)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_stage, b->stage_bytes)) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_counter, sizeof(unsigned int))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_out, (size_t)max_pixels * sizeof(float))) != cudaSuccess ||
+      (e = cudaHostAlloc(&b->h_out, (size_t)max_pixels * sizeof(float), cudaHostAllocDefault)) != cudaSuccess ||
+      (e = cudaEventCreate(&b->e_start)) != cudaSuccess || (e = cudaEventCreate(&b->e_kernel)) != cudaSuccess ||
+      (e = cudaEventCreate(&b->e_end)) != cudaSuccess)
+    return bail(fail(e == cudaErrorMemoryAllocation ? BIRP_ERR_NOMEM : BIRP_ERR_CUDA, "batch allocation: %s",
+                     cudaGetErrorString(e)));
+  std::memset(b->h_stage, 0, b->stage_bytes);
+
+  BatchDev bd;
+  bd.hdr = reinterpret_cast<const int*>(b->d_stage);
+  bd.first = reinterpret_cast<const int*>(b->d_stage + b->off_first);
+  bd.order = reinterpret_cast<const int*>(b->d_stage + b->off_order);
+  bd.reqs = reinterpret_cast<const RequestDev*>(b->d_stage + b->off_reqs);
+  bd.counter = b->d_counter;
+  bd.stats = g_ctx.stats;
+  b->grid = persistent_grid(0);
+
+  // capture: descriptors H2D, queue head reset, persistent kernel
+  if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+  cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
+  cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), b->stream);
+  launch_render_batch(bd, b->grid, b->stream);
+  e = cudaStreamEndCapture(b->stream, &b->graph);
+  if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+  if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess)
+    return bail(fail(BIRP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  *out = b;
+  return ok();
+}
+
+birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n) {
+  if (birp_status s = check_init()) return s;
+  if (!b || n < 0 || (n > 0 && !reqs)) return fail(BIRP_ERR_INVALID, "bad argument");
+  if (n > b->max_req) return fail(BIRP_ERR_INVALID, "%d requests exceed the batch limit %d", n, b->max_req);
+  if (b->pending)
+    if (birp_status s = batch_wait(b)) return s;
+  int* hdr = reinterpret_cast<int*>(b->h_stage);
+  int* first = reinterpret_cast<int*>(b->h_stage + b->off_first);
+  int* order = reinterpret_cast<int*>(b->h_stage + b->off_order);
+  RequestDev* rq = reinterpret_cast<RequestDev*>(b->h_stage + b->off_reqs);
+  b->offsets.assign(n, 0);
+  b->npx.assign(n, 0);
+  int64_t used = 0;
+  std::vector<double> work(n);
+  for (int i = 0; i < n; ++i) {
+    const birp_camera& c = reqs[i].cam;
+    if (birp_status s = validate_camera(&c)) return s;
+    int64_t npx = (int64_t)c.nx * c.ny;
+    if (used + npx > b->max_px)
+      return fail(BIRP_ERR_INVALID, "batch images need more than %lld pixels", (long long)b->max_px);
+    b->offsets[i] = used;
+    b->npx[i] = npx;
+    if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, b->d_out + used, rq[i])) return s;
+    used += npx;
+    work[i] = (double)npx * c.n_samples * (reqs[i].cmem ? 16.0 : 1.0);
+  }
+  // largest work first, so long renders start early and small ones fill the tail
+  std::iota(order, order + n, 0);
+  std::stable_sort(order, order + n, [&](int x, int y) { return work[x] > work[y]; });
+  first[0] = 0;
+  for (int k = 0; k < n; ++k) first[k + 1] = first[k] + rq[order[k]].tiles;
+  hdr[0] = n;
+  hdr[1] = first[n];
+  b->n = n;
+  b->used = used;
+  cudaError_t e;
+  if ((e = cudaEventRecord(b->e_start, b->stream)) != cudaSuccess ||
+      (e = cudaGraphLaunch(b->exec, b->stream)) != cudaSuccess ||
+      (e = cudaEventRecord(b->e_kernel, b->stream)) != cudaSuccess ||
+      (used > 0 && (e = cudaMemcpyAsync(b->h_out, b->d_out, (size_t)used * sizeof(float), cudaMemcpyDeviceToHost,
+                                        b->stream)) != cudaSuccess) ||
+      (e = cudaEventRecord(b->e_end, b->stream)) != cudaSuccess)
+    return fail(BIRP_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
+  b->pending = true;
+  return ok();
+}
+
+birp_status batch_wait(birp_batch* b) {
+  if (!b) return fail(BIRP_ERR_INVALID, "NULL batch");
+  if (!b->pending) return ok();
+  cudaError_t e = cudaEventSynchronize(b->e_end);
+  b->pending = false;
+  if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "batch: %s", cudaGetErrorString(e));
+  return ok();
+}
+
+}  // namespace birp
+
+extern "C" {
+
+birp_status birp_batch_create(int max_requests, int64_t max_pixels, birp_batch** out) {
+  return batch_create(max_requests, max_pixels, out);
+}
+
+birp_status birp_batch_destroy(birp_batch* b) {
+  free_batch(b);
+  return ok();
+}
+
+birp_status birp_batch_submit(birp_batch* b, const birp_request* reqs, int n) { return batch_submit(b, reqs, n); }
+
+birp_status birp_batch_wait(birp_batch* b) { return batch_wait(b); }
+
+const float* birp_batch_image(const birp_batch* b, int i) {
+  if (!b || i < 0 || i >= b->n || b->pending) return nullptr;
+  return b->h_out + b->offsets[i];
+}
+
+birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, float* const* outs) {
+  if (n > 0 && !outs) return fail(BIRP_ERR_INVALID, "outs is NULL");
+  if (birp_status s = batch_submit(b, reqs, n)) return s;
+  if (birp_status s = batch_wait(b)) return s;
+  for (int i = 0; i < n; ++i)
+    if (outs[i]) std::memcpy(outs[i], b->h_out + b->offsets[i], (size_t)b->npx[i] * sizeof(float));
+  return ok();
+}
+
+birp_status birp_batch_last_ms(const birp_batch* b, float* kernel_ms, float* total_ms) {
+  if (!b || b->pending) return fail(BIRP_ERR_INVALID, "no finished launch");
+  float k = 0, t = 0;
+  CKB(cudaEventElapsedTime(&k, b->e_start, b->e_kernel));
+  CKB(cudaEventElapsedTime(&t, b->e_start, b->e_end));
+  if (kernel_ms) *kernel_ms = k;
+  if (total_ms) *total_ms = t;
+  return ok();
+}
+
+}  // extern "C"

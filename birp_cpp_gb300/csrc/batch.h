@@ -1,0 +1,32 @@
+// Batch object shared by the batch C ABI and the server.
+#pragma once
+#include <vector>
+
+#include "birp_host.h"
+
+struct birp_batch {
+  int max_req = 0;
+  int64_t max_px = 0;
+  size_t off_first = 0, off_order = 0, off_reqs = 0, stage_bytes = 0;
+  char* h_stage = nullptr;   // pinned descriptors of the next launch
+  char* d_stage = nullptr;
+  unsigned int* d_counter = nullptr;
+  float* d_out = nullptr;    // images of the launch, concatenated
+  float* h_out = nullptr;    // pinned copy of the images
+  std::vector<int64_t> offsets;
+  std::vector<int64_t> npx;
+  int n = 0;
+  int64_t used = 0;
+  int grid = 0;
+  bool pending = false;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaEvent_t e_start = nullptr, e_kernel = nullptr, e_end = nullptr;
+};
+
+namespace birp {
+birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out);
+birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n);
+birp_status batch_wait(birp_batch* b);
+}  // namespace birp

@@ -1,0 +1,79 @@
+// Host-side internals shared by the C ABI translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "../../include/birp_gb300.h"
+#include "birp_internal.h"
+
+// Opaque handle types of the C ABI.
+struct birp_cube {
+  int n[3] = {0, 0, 0};
+  std::vector<double> c[3];     // host copies of the axes
+  int uniform[3] = {0, 0, 0};
+  double inv_h[3] = {0, 0, 0};  // uniform axes: 1 / spacing
+  double min_gap[3] = {0, 0, 0};
+  birp::CubeDev h_desc{};       // host copy of the device descriptor
+  birp::CubeDev* d_desc = nullptr;
+  float* d_vals = nullptr;
+  double* d_c64 = nullptr;      // 3 axes, concatenated
+  float4* d_lut = nullptr;
+  size_t device_bytes = 0;
+  cudaStream_t alloc_stream = nullptr;  // non-null: stream-ordered (pool) allocations
+};
+
+struct birp_cmem {
+  birp::CmemDev h_desc{};
+  birp::CmemDev* d_desc = nullptr;
+};
+
+namespace birp {
+
+// Library context: one device per process.
+struct Context {
+  int device = -1;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  KernelStats* stats = nullptr;
+  float* scratch = nullptr;      // image buffer of birp_render
+  size_t scratch_floats = 0;
+  float* xyz_scratch = nullptr;  // point-sample buffers
+  size_t xyz_floats = 0;
+  void* flush = nullptr;         // L2 flush buffer (timing)
+  std::mutex mu;
+};
+extern Context g_ctx;
+
+// FP64 camera frame (see camera_frame in capi.cu).
+struct Frame {
+  double rinv[3][3];
+  double tfx, tfy, aspect, dt, K, angle_sun;
+};
+
+birp_status fail(birp_status s, const char* fmt, ...);
+birp_status ok();
+birp_status check_init();
+birp_status validate_camera(const birp_camera* c);
+birp_status camera_frame(const birp_camera& c, Frame& f);
+birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const birp_camera& c, float* out,
+                          RequestDev& r);
+cudaStream_t pick_stream(void* s);
+
+// cube.cu
+birp_status analyze_axis(const double* c, int n, char name, birp_cube& cube, int k);
+birp_status upload_cube(birp_cube& cube, const float* values, cudaStream_t stream, bool stream_alloc);
+// estimate of the device bytes a cube of these dims will hold
+size_t cube_device_bytes(const birp_cube& cube);
+void destroy_cube_device(birp_cube& cube);
+birp_status ensure_xyz_scratch(size_t floats);
+
+// cmem_host.cpp
+void cmem_coefficients(const birp_cmem_params& p, CmemDev& m);
+
+// tune.cpp: lanes-per-ray choice from the committed tuning table
+int tuned_seg_log2(int64_t pixels, int n_samples, int kind, int trilinear);
+
+}  // namespace birp

@@ -1,0 +1,119 @@
+// Internal host/device structures of the GB300 render path.
+//
+// Data layout in HBM (one cube):
+//  * values: FP32, x fastest, padded by one guard node on every side
+//    (dims (nx+2) x (ny+2) x (nz+2)); a guard node repeats its edge neighbour,
+//    so a cell index that FP32 rounding puts one step outside [0, n-2] still
+//    reads in-bounds memory and interpolates continuously.
+//  * per-axis index tables (LUT) for nonuniform axes: float4 bins of width at
+//    most the smallest cell, each holding one piecewise-linear index map.
+//  * FP64 axis coordinates, read only by the exact (FP64) decisions.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace birp {
+
+constexpr int kMaxLutBins = 1 << 16;  // per axis
+
+// One axis of a cube.
+struct AxisDev {
+  int n;            // nodes
+  int uniform;      // 1: idx = (x - c0) * inv_h (affine); 0: LUT
+  float c0;         // first node (FP32)
+  float inv_h;      // 1 / spacing (uniform)
+  float lut_x0;     // LUT origin (FP32 of c[0])
+  float lut_inv_w;  // 1 / bin width
+  int lut_n;        // bins
+  int lut_off;      // offset of this axis' bins in CubeDev::lut
+  double c_first;   // c[0]  (FP64)
+  double c_last;    // c[n-1] (FP64)
+  const double* c64;  // n FP64 node coordinates (device)
+};
+
+struct CubeDev {
+  AxisDev ax[3];
+  const float* vals;    // guard-padded grid (see above)
+  uint32_t px;          // nx + 2
+  uint32_t pxy;         // (nx + 2) * (ny + 2)
+  uint32_t max_off;     // largest valid base offset for an 8-corner fetch
+  uint32_t bias;        // folds the FP32 magic-floor bias and the guard shift
+  int all_uniform;
+  const float4* lut;    // concatenated LUT bins (nullptr if all uniform)
+};
+
+// CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
+struct CmemDev {
+  float p0r0, p1, p2c, p3dn, p3ds, a5, a21, bs, ay, az, A1, A2, B, alpha, beta;
+  float bc0, bc1, bc3, cos_tn, sin_tn, cos_ts, sin_ts;
+  double d_p0, d_p1, d_p2, d_p3, d_dn, d_ds, d_tn, d_ts, d_r0, d_charlie, d_a5, d_a21;
+  double d_bs, d_ay, d_az, d_A1, d_A2, d_B, d_alpha, d_beta, d_bc0, d_bc1, d_bc3;
+  float eps_rel;  // FP32 boundary-decision margin (relative to r)
+};
+
+enum SpaceKind : int { SPACE_CUBE = 0, SPACE_CMEM = 1 };
+enum MarchMode : int { MARCH_PREFIX = 0, MARCH_CLIP = 1 };
+
+// One render request as the kernels see it (per camera).
+struct RequestDev {
+  // FP64 frame: exactly the FP64 oracle's pose (R^-1, tan(fov/2), aspect)
+  double rinv[3][3];
+  double tfx, tfy, aspect;
+  double pos[3];
+  double dt;
+  double K;          // per-sample scale (src/Camera.cpp:201 with ray_width = dt)
+  float pos32[3];
+  float dt32;
+  int nx, ny, N;
+  int mode;          // MarchMode
+  int interp;        // 1 trilinear, 0 nearest
+  int kind;          // SpaceKind
+  int seg_log2;      // rays are split over 2^seg_log2 lanes
+  int tiles_x;       // tiles along x for this request's tile shape
+  int tiles;         // total tiles
+  int axes_lut;      // cube: 1 when any axis needs the LUT
+  const CubeDev* cube;   // device pointer (kind == SPACE_CUBE)
+  const CmemDev* cmem;   // device pointer (kind == SPACE_CMEM)
+  float* out;            // ny*nx floats, row 0 = top
+  float oidx[3];         // (pos - c0) * inv_h for uniform axes
+};
+
+// Status/counters the kernels report (device memory, read by the host).
+struct KernelStats {
+  unsigned long long exact_range_rays;   // rays whose in-box range needed FP64
+  unsigned long long exact_nearest;      // nearest-mode samples decided in FP64
+  unsigned long long exact_cmem;         // CMEM samples decided in FP64
+  unsigned long long items;              // work items rendered (persistent kernel)
+  unsigned long long samples;            // ray-samples evaluated
+  unsigned int error;                    // nonzero: a device-side consistency check failed
+  unsigned int error_info;
+};
+
+// Work item table of a batch: request r owns items [first[r], first[r+1]).
+// The pointers are fixed for the life of a batch object (so a captured CUDA
+// graph stays valid); the sizes of each launch are read from device memory.
+struct BatchDev {
+  const RequestDev* reqs;
+  const int* first;        // n_reqs + 1 prefix sums of tiles, in launch order
+  const int* order;        // request index of each launch position (largest work first)
+  const int* hdr;          // {n_reqs, total_items}
+  unsigned int* counter;   // work queue head (zeroed before each launch)
+  KernelStats* stats;
+};
+
+// Host-side launch helpers (render.cu).
+cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaStream_t stream);
+cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream);
+int persistent_grid(int seg_mix_max);
+cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
+cudaError_t launch_cube_sample(const CubeDev* cube, int trilinear, const float* xyz, int n, float* out,
+                               cudaStream_t stream);
+cudaError_t launch_cmem_sample(const CmemDev* cmem, const float* xyz, int n, float* out, cudaStream_t stream);
+cudaError_t launch_cmem_radii_check(const CmemDev* cmem, int n, unsigned long long seed, float* max_err,
+                                    cudaStream_t stream);
+cudaError_t launch_peak_fp32(float* sink, int blocks, int iters, cudaStream_t stream);
+cudaError_t launch_peak_read(const float4* buf, size_t n4, int reps, float* sink, int blocks, cudaStream_t stream);
+int tile_w(int seg_log2);
+int tile_h(int seg_log2);
+
+}  // namespace birp

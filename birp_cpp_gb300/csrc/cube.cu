@@ -1,0 +1,203 @@
+// DataCube upload: axis analysis, index tables for nonuniform axes and the
+// guard-padded FP32 grid in HBM (layout in birp_internal.h). Replaces the
+// state DataCube::Load / InitSpacing / InitOriginCoords / InitSize leave
+// behind (src/DataCube.cpp:28-197).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "birp_host.h"
+
+namespace birp {
+
+birp_status analyze_axis(const double* c, int n, char name, birp_cube& cube, int k) {
+  if (n < 2) return fail(BIRP_ERR_INVALID, "axis %c needs at least 2 nodes (got %d)", name, n);
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(c[i])) return fail(BIRP_ERR_INVALID, "axis %c node %d is not finite", name, i);
+  double min_gap = INFINITY;
+  for (int i = 1; i < n; ++i) {
+    double g = c[i] - c[i - 1];
+    if (!(g > 0)) return fail(BIRP_ERR_INVALID, "axis %c must be strictly increasing (node %d)", name, i);
+    min_gap = std::min(min_gap, g);
+  }
+  const double h = (c[n - 1] - c[0]) / (n - 1);
+  bool uniform = true;
+  for (int i = 1; i < n && uniform; ++i) uniform = std::abs((c[i] - c[i - 1]) - h) <= 1e-6 * h;
+  cube.n[k] = n;
+  cube.c[k].assign(c, c + n);
+  cube.uniform[k] = uniform ? 1 : 0;
+  cube.inv_h[k] = 1.0 / h;
+  cube.min_gap[k] = min_gap;
+  const double span = c[n - 1] - c[0];
+  if (span / min_gap > (double)kMaxLutBins)
+    return fail(BIRP_ERR_INVALID, "axis %c: span / smallest cell = %.0f exceeds %d", name, span / min_gap,
+                kMaxLutBins);
+  return BIRP_OK;
+}
+
+// Index table of one axis: bins of width w = the smallest cell; bin b covers
+// [c0 + b w, c0 + (b+1) w) and holds {xk, kk, s0, s1} with the continuous index
+// idx(x) = kk + (x - xk) * (x < xk ? s0 : s1): xk is the one node strictly
+// inside the bin (if any; else the node below the bin start), kk its index,
+// s0/s1 the inverse widths of the cells left/right of it.
+static void build_lut(const std::vector<double>& c, double w, std::vector<float4>& lut) {
+  const int n = (int)c.size();
+  const int nb = std::max(1, (int)std::ceil((c[n - 1] - c[0]) / w));
+  lut.resize(nb);
+  int k = 0;
+  for (int b = 0; b < nb; ++b) {
+    const double xb = c[0] + b * w;
+    while (k < n - 2 && c[k + 1] <= xb) ++k;
+    double xk, s0, s1;
+    int kk;
+    const double inv_k = 1.0 / (c[k + 1] - c[k]);
+    if (c[k + 1] > xb && c[k + 1] < xb + w) {
+      xk = c[k + 1];
+      kk = k + 1;
+      s0 = inv_k;
+      s1 = (k + 2 <= n - 1) ? 1.0 / (c[k + 2] - c[k + 1]) : inv_k;
+    } else {
+      xk = c[k];
+      kk = k;
+      s0 = s1 = inv_k;
+    }
+    lut[b] = make_float4((float)xk, (float)kk, (float)s0, (float)s1);
+  }
+}
+
+birp_status ensure_xyz_scratch(size_t floats) {
+  Context& g = g_ctx;
+  if (g.xyz_floats >= floats) return BIRP_OK;
+  if (g.xyz_scratch) cudaFree(g.xyz_scratch);
+  g.xyz_scratch = nullptr;
+  g.xyz_floats = 0;
+  size_t want = std::max(floats, (size_t)1 << 16);
+  cudaError_t e = cudaMalloc(&g.xyz_scratch, want * sizeof(float));
+  if (e != cudaSuccess) return fail(BIRP_ERR_NOMEM, "cudaMalloc: %s", cudaGetErrorString(e));
+  g.xyz_floats = want;
+  return BIRP_OK;
+}
+
+void destroy_cube_device(birp_cube& c) {
+  if (c.alloc_stream) {
+    // stream-ordered pool memory: no device-wide synchronisation on release
+    for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc})
+      if (p) cudaFreeAsync(p, c.alloc_stream);
+  } else {
+    if (c.d_vals) cudaFree(c.d_vals);
+    if (c.d_c64) cudaFree(c.d_c64);
+    if (c.d_lut) cudaFree(c.d_lut);
+    if (c.d_desc) cudaFree(c.d_desc);
+  }
+  c.d_vals = nullptr;
+  c.d_c64 = nullptr;
+  c.d_lut = nullptr;
+  c.d_desc = nullptr;
+}
+
+#define CKU(x)                                                                                 \
+  do {                                                                                         \
+    cudaError_t e_ = (x);                                                                      \
+    if (e_ != cudaSuccess)                                                                     \
+      return fail(e_ == cudaErrorMemoryAllocation ? BIRP_ERR_NOMEM : BIRP_ERR_CUDA, "%s: %s", #x, \
+                  cudaGetErrorString(e_));                                                     \
+  } while (0)
+
+template <class T>
+static cudaError_t dev_alloc(T** p, size_t bytes, cudaStream_t alloc_stream) {
+  return alloc_stream ? cudaMallocAsync((void**)p, bytes, alloc_stream) : cudaMalloc((void**)p, bytes);
+}
+
+birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool stream_alloc) {
+  const int nx = c.n[0], ny = c.n[1], nz = c.n[2];
+  const size_t px = (size_t)nx + 2, py = (size_t)ny + 2, pz = (size_t)nz + 2;
+  const size_t total = px * py * pz;
+  if (!st) st = g_ctx.stream;
+  c.alloc_stream = stream_alloc ? st : nullptr;
+
+  CubeDev& d = c.h_desc;
+  std::memset(&d, 0, sizeof d);
+  d.all_uniform = (c.uniform[0] && c.uniform[1] && c.uniform[2]) ? 1 : 0;
+
+  // index tables for every axis when any axis is nonuniform
+  std::vector<float4> lut;
+  int lut_off[3] = {0, 0, 0}, lut_n[3] = {0, 0, 0};
+  if (!d.all_uniform) {
+    for (int k = 0; k < 3; ++k) {
+      std::vector<float4> one;
+      build_lut(c.c[k], c.min_gap[k], one);
+      lut_off[k] = (int)lut.size();
+      lut_n[k] = (int)one.size();
+      lut.insert(lut.end(), one.begin(), one.end());
+    }
+  }
+
+  size_t coords = (size_t)nx + ny + nz;
+  CKU(dev_alloc(&c.d_vals, total * sizeof(float), c.alloc_stream));
+  CKU(dev_alloc(&c.d_c64, coords * sizeof(double), c.alloc_stream));
+  if (!lut.empty()) CKU(dev_alloc(&c.d_lut, lut.size() * sizeof(float4), c.alloc_stream));
+  CKU(dev_alloc(&c.d_desc, sizeof(CubeDev), c.alloc_stream));
+  c.device_bytes = total * sizeof(float) + coords * sizeof(double) + lut.size() * sizeof(float4) + sizeof(CubeDev);
+
+  // interior values: one strided 3D copy from the caller's x-fastest array
+  cudaMemcpy3DParms p;
+  std::memset(&p, 0, sizeof p);
+  p.srcPtr = make_cudaPitchedPtr((void*)values, (size_t)nx * sizeof(float), nx, ny);
+  p.dstPtr = make_cudaPitchedPtr(c.d_vals, px * sizeof(float), px, py);
+  p.dstPos = make_cudaPos(sizeof(float), 1, 1);
+  p.extent = make_cudaExtent((size_t)nx * sizeof(float), ny, nz);
+  p.kind = cudaMemcpyHostToDevice;
+  CKU(cudaMemcpy3DAsync(&p, st));
+  CKU(launch_cube_fill(nullptr, nx, ny, nz, c.d_vals, st));
+
+  // (the host vectors below stay alive until the synchronize at the end)
+  std::vector<double> all;
+  all.reserve(coords);
+  for (int k = 0; k < 3; ++k) all.insert(all.end(), c.c[k].begin(), c.c[k].end());
+  CKU(cudaMemcpyAsync(c.d_c64, all.data(), coords * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (!lut.empty()) CKU(cudaMemcpyAsync(c.d_lut, lut.data(), lut.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+
+  size_t off = 0;
+  for (int k = 0; k < 3; ++k) {
+    AxisDev& a = d.ax[k];
+    const std::vector<double>& ck = c.c[k];
+    a.n = c.n[k];
+    a.uniform = c.uniform[k];
+    a.c0 = (float)ck[0];
+    a.inv_h = (float)c.inv_h[k];
+    a.lut_x0 = (float)ck[0];
+    a.lut_inv_w = (float)(1.0 / c.min_gap[k]);
+    a.lut_n = lut_n[k];
+    a.lut_off = lut_off[k];
+    a.c_first = ck[0];
+    a.c_last = ck[a.n - 1];
+    a.c64 = c.d_c64 + off;
+    off += a.n;
+  }
+  d.vals = c.d_vals;
+  d.px = (uint32_t)px;
+  d.pxy = (uint32_t)(px * py);
+  const uint32_t corner = d.pxy + d.px + 1;  // offset of node (0,0,0) in the padded grid
+  d.bias = (uint32_t)((1u - (uint32_t)0x4B400000) * corner);
+  d.max_off = (uint32_t)(total - 1 - corner);
+  d.lut = c.d_lut;
+  CKU(cudaMemcpyAsync(c.d_desc, &d, sizeof d, cudaMemcpyHostToDevice, st));
+  CKU(cudaStreamSynchronize(st));
+  return BIRP_OK;
+}
+
+}  // namespace birp
+
+namespace birp {
+size_t cube_device_bytes(const birp_cube& c) {
+  const size_t total = ((size_t)c.n[0] + 2) * ((size_t)c.n[1] + 2) * ((size_t)c.n[2] + 2);
+  const size_t coords = (size_t)c.n[0] + c.n[1] + c.n[2];
+  const bool all_uniform = c.uniform[0] && c.uniform[1] && c.uniform[2];
+  size_t lut = 0;
+  if (!all_uniform)
+    for (int k = 0; k < 3; ++k)
+      lut += (size_t)std::max(1.0, std::ceil((c.c[k].back() - c.c[k].front()) / c.min_gap[k])) * sizeof(float4);
+  return total * sizeof(float) + coords * sizeof(double) + lut + sizeof(CubeDev);
+}
+}  // namespace birp

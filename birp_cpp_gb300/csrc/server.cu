@@ -1,0 +1,473 @@
+// Continuous-batching render server (birp_server_* in include/birp_gb300.h).
+//
+// Requests are admitted as they arrive. A scheduler thread forms a batch from
+// the pending queue whenever a slot (a batch object with its own stream and
+// CUDA graph) is free, making each batch's cubes resident first: cubes live in
+// GPU memory under a byte budget, least-recently-used cubes that no in-flight
+// batch references are evicted, and a missing cube is re-uploaded from its
+// pinned host copy on a separate stream (stream-ordered pool allocations, so
+// neither upload nor eviction synchronises the device). Batches on different
+// slots overlap on the GPU. One completion thread per slot waits for its
+// batch, copies each image to the caller's buffer and completes the tickets.
+// The reference has no counterpart: its only "many renders" path is the
+// serial directory loop of src/main.cpp:242-264.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "batch.h"
+
+using namespace birp;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_since(Clock::time_point t0, Clock::time_point t1) {
+  return std::chrono::duration<double, std::milli>(t1 - t0).count();
+}
+
+struct Source {
+  int kind = 0;  // 0 cube, 1 cmem
+  std::vector<double> ax[3];
+  float* h_vals = nullptr;  // pinned host copy (cubes)
+  int64_t bytes = 0;        // device bytes when resident
+  birp_cube* resident = nullptr;
+  uint64_t last_use = 0;
+  int in_use = 0;           // batches (forming or in flight) that reference it
+  birp_cmem* cmem = nullptr;
+};
+
+struct Req {
+  int64_t ticket = 0;
+  int src = 0;
+  birp_camera cam{};
+  float* out = nullptr;
+  Clock::time_point t_submit, t_launch, t_done;
+  birp_status status = BIRP_OK;
+  bool done = false;
+};
+
+struct Slot {
+  birp_batch* batch = nullptr;
+  std::vector<Req*> reqs;
+  std::vector<int> srcs;  // distinct sources pinned by this batch
+  bool busy = false;
+  bool has_work = false;
+  std::condition_variable cv;
+  std::thread worker;
+};
+
+}  // namespace
+
+struct birp_server {
+  birp_server_config cfg{};
+  std::mutex mu;
+  std::condition_variable cv_sched, cv_done;
+  std::deque<Req*> pending;
+  std::unordered_map<int64_t, Req*> tickets;
+  std::vector<Source> sources;
+  std::vector<Slot*> slots;
+  std::thread scheduler;
+  bool stop = false;
+  int64_t next_ticket = 1;
+  uint64_t tick = 0;
+  int64_t resident_bytes = 0;
+  cudaStream_t upload_stream = nullptr;
+  birp_server_stats st{};
+};
+
+namespace {
+
+void finish(birp_server* s, Req* r, birp_status status) {
+  r->status = status;
+  r->t_done = Clock::now();
+  r->done = true;
+}
+
+// Makes source `id` resident; called with the lock held, releases it around
+// the upload itself. Returns BIRP_OK or an error for the requests of `id`.
+birp_status make_resident(birp_server* s, int id, std::unique_lock<std::mutex>& lk) {
+  Source& src = s->sources[id];
+  src.last_use = ++s->tick;
+  if (src.kind != 0) return BIRP_OK;
+  if (src.resident) {
+    s->st.cube_hits++;
+    return BIRP_OK;
+  }
+  if (src.bytes > s->cfg.cube_budget_bytes)
+    return fail(BIRP_ERR_NOMEM, "cube needs %lld B, budget is %lld B", (long long)src.bytes,
+                (long long)s->cfg.cube_budget_bytes);
+  // evict least-recently-used cubes that no batch references
+  while (s->resident_bytes + src.bytes > s->cfg.cube_budget_bytes) {
+    int victim = -1;
+    for (int i = 0; i < (int)s->sources.size(); ++i) {
+      const Source& o = s->sources[i];
+      if (i == id || !o.resident || o.in_use > 0) continue;
+      if (victim < 0 || o.last_use < s->sources[victim].last_use) victim = i;
+    }
+    if (victim < 0) return fail(BIRP_ERR_BUSY, "cube budget held by in-flight batches");
+    Source& v = s->sources[victim];
+    birp_cube* c = v.resident;
+    v.resident = nullptr;
+    s->resident_bytes -= v.bytes;
+    s->st.cube_evictions++;
+    destroy_cube_device(*c);  // stream-ordered release on the upload stream
+    delete c;
+  }
+  // upload outside the lock (the source is pinned by in_use)
+  birp_cube* c = new birp_cube();
+  birp_status rc = BIRP_OK;
+  s->resident_bytes += src.bytes;
+  const float* vals = src.h_vals;
+  std::vector<double> ax[3] = {src.ax[0], src.ax[1], src.ax[2]};
+  lk.unlock();
+  for (int k = 0; k < 3 && rc == BIRP_OK; ++k) rc = analyze_axis(ax[k].data(), (int)ax[k].size(), "xyz"[k], *c, k);
+  if (rc == BIRP_OK) rc = upload_cube(*c, vals, s->upload_stream, true);
+  lk.lock();
+  if (rc != BIRP_OK) {
+    s->resident_bytes -= src.bytes;
+    destroy_cube_device(*c);
+    delete c;
+    return rc;
+  }
+  s->resident_bytes += (int64_t)c->device_bytes - src.bytes;
+  src.bytes = (int64_t)c->device_bytes;
+  src.resident = c;
+  s->st.cube_uploads++;
+  return BIRP_OK;
+}
+
+void slot_worker(birp_server* s, Slot* slot) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  for (;;) {
+    slot->cv.wait(lk, [&] { return slot->has_work || s->stop; });
+    if (!slot->has_work) return;
+    lk.unlock();
+    birp_status rc = batch_wait(slot->batch);
+    // copy images to the callers' buffers (outside the lock)
+    if (rc == BIRP_OK)
+      for (size_t i = 0; i < slot->reqs.size(); ++i)
+        std::memcpy(slot->reqs[i]->out, slot->batch->h_out + slot->batch->offsets[i],
+                    (size_t)slot->batch->npx[i] * sizeof(float));
+    lk.lock();
+    for (Req* r : slot->reqs) finish(s, r, rc);
+    s->st.completed += (int64_t)slot->reqs.size();
+    for (int id : slot->srcs) s->sources[id].in_use--;
+    slot->reqs.clear();
+    slot->srcs.clear();
+    slot->has_work = false;
+    slot->busy = false;
+    s->cv_done.notify_all();
+    s->cv_sched.notify_all();
+  }
+}
+
+void scheduler_loop(birp_server* s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  const auto window = std::chrono::duration<double, std::milli>(s->cfg.max_wait_ms);
+  while (!s->stop) {
+    Slot* slot = nullptr;
+    bool any_busy = false;
+    for (Slot* sl : s->slots) {
+      if (!sl->busy && !slot) slot = sl;
+      any_busy |= sl->busy;
+    }
+    if (!slot || s->pending.empty()) {
+      s->cv_sched.wait(lk);
+      continue;
+    }
+    // batching window: while the GPU is busy, let a small batch fill up a little
+    if (any_busy && (int)s->pending.size() < s->cfg.max_batch_requests) {
+      auto deadline = s->pending.front()->t_submit + std::chrono::duration_cast<Clock::duration>(window);
+      if (Clock::now() < deadline) {
+        s->cv_sched.wait_until(lk, deadline);
+        continue;
+      }
+    }
+    // form a batch in arrival order
+    std::vector<Req*> take;
+    std::vector<int> srcs;
+    int64_t px = 0;
+    std::deque<Req*> keep;
+    while (!s->pending.empty() && (int)take.size() < s->cfg.max_batch_requests) {
+      Req* r = s->pending.front();
+      int64_t n = (int64_t)r->cam.nx * r->cam.ny;
+      if (n > s->cfg.max_batch_pixels) {  // can never fit
+        s->pending.pop_front();
+        fail(BIRP_ERR_INVALID, "image larger than the batch pixel limit");
+        finish(s, r, BIRP_ERR_INVALID);
+        s->cv_done.notify_all();
+        continue;
+      }
+      if (px + n > s->cfg.max_batch_pixels) break;
+      s->pending.pop_front();
+      take.push_back(r);
+      px += n;
+      if (std::find(srcs.begin(), srcs.end(), r->src) == srcs.end()) {
+        srcs.push_back(r->src);
+        s->sources[r->src].in_use++;
+      }
+    }
+    if (take.empty()) continue;
+    slot->busy = true;  // reserve the slot while cubes upload
+    // residency
+    std::vector<char> src_ok(s->sources.size(), 1);
+    std::vector<birp_status> src_err(s->sources.size(), BIRP_OK);
+    for (int id : srcs) {
+      birp_status rc = make_resident(s, id, lk);
+      if (rc == BIRP_ERR_BUSY) {
+        // budget held by other batches: retry these requests later
+        src_ok[id] = 0;
+      } else if (rc != BIRP_OK) {
+        src_ok[id] = 0;
+        src_err[id] = rc;
+      }
+    }
+    std::vector<Req*> go;
+    std::vector<birp_request> reqs;
+    for (Req* r : take) {
+      if (src_ok[r->src]) {
+        go.push_back(r);
+        continue;
+      }
+      if (src_err[r->src] != BIRP_OK) {
+        finish(s, r, src_err[r->src]);
+        s->st.completed++;
+      } else {
+        keep.push_back(r);
+      }
+    }
+    for (auto it = keep.rbegin(); it != keep.rend(); ++it) s->pending.push_front(*it);
+    std::vector<int> used_srcs;
+    for (int id : srcs) {
+      bool used = std::any_of(go.begin(), go.end(), [&](Req* r) { return r->src == id; });
+      if (used) used_srcs.push_back(id);
+      else s->sources[id].in_use--;
+    }
+    s->cv_done.notify_all();
+    if (go.empty()) {
+      slot->busy = false;
+      if (!keep.empty()) s->cv_sched.wait_for(lk, std::chrono::milliseconds(1));
+      continue;
+    }
+    for (Req* r : go) {
+      birp_request q{};
+      const Source& src = s->sources[r->src];
+      q.cube = src.kind == 0 ? src.resident : nullptr;
+      q.cmem = src.kind == 1 ? src.cmem : nullptr;
+      q.cam = r->cam;
+      reqs.push_back(q);
+    }
+    const auto now = Clock::now();
+    birp_status rc = batch_submit(slot->batch, reqs.data(), (int)reqs.size());
+    for (Req* r : go) r->t_launch = now;
+    s->st.batches++;
+    slot->reqs = go;
+    slot->srcs = used_srcs;
+    if (rc != BIRP_OK) {
+      for (Req* r : go) finish(s, r, rc);
+      s->st.completed += (int64_t)go.size();
+      for (int id : used_srcs) s->sources[id].in_use--;
+      slot->reqs.clear();
+      slot->srcs.clear();
+      slot->busy = false;
+      s->cv_done.notify_all();
+      continue;
+    }
+    slot->has_work = true;
+    slot->cv.notify_one();
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void birp_server_default_config(birp_server_config* c) {
+  if (!c) return;
+  c->cube_budget_bytes = (int64_t)60 << 30;
+  c->slots = 3;
+  c->max_batch_requests = 64;
+  c->max_batch_pixels = (int64_t)8 << 20;
+  c->max_queue = 1 << 16;
+  c->max_wait_ms = 1.0;
+}
+
+birp_status birp_server_create(const birp_server_config* cfg, birp_server** out) {
+  if (birp_status e = check_init()) return e;
+  if (!out) return fail(BIRP_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  birp_server_config c;
+  birp_server_default_config(&c);
+  if (cfg) c = *cfg;
+  if (c.slots < 1 || c.slots > 16 || c.max_batch_requests < 1 || c.max_batch_pixels < 1 || c.max_queue < 1 ||
+      c.cube_budget_bytes < 0 || !(c.max_wait_ms >= 0))
+    return fail(BIRP_ERR_INVALID, "bad server configuration");
+  birp_server* s = new birp_server();
+  s->cfg = c;
+  cudaError_t e = cudaStreamCreateWithFlags(&s->upload_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(BIRP_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+  }
+  // keep freed cube memory in the process's pool for reuse (no release to the
+  // driver between evictions); a per-process setting of this library's pool
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, g_ctx.device) == cudaSuccess) {
+    uint64_t keep = (uint64_t)c.cube_budget_bytes;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  for (int i = 0; i < c.slots; ++i) {
+    Slot* sl = new Slot();
+    birp_status rc = batch_create(c.max_batch_requests, c.max_batch_pixels, &sl->batch);
+    if (rc != BIRP_OK) {
+      delete sl;
+      birp_server_destroy(s);
+      return rc;
+    }
+    s->slots.push_back(sl);
+  }
+  for (Slot* sl : s->slots) sl->worker = std::thread(slot_worker, s, sl);
+  s->scheduler = std::thread(scheduler_loop, s);
+  *out = s;
+  return ok();
+}
+
+birp_status birp_server_destroy(birp_server* s) {
+  if (!s) return ok();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv_sched.notify_all();
+    for (Slot* sl : s->slots) sl->cv.notify_all();
+  }
+  if (s->scheduler.joinable()) s->scheduler.join();
+  for (Slot* sl : s->slots) {
+    // a batch still in flight is waited for by its worker before it exits
+    {
+      std::unique_lock<std::mutex> lk(s->mu);
+      sl->cv.notify_all();
+    }
+    if (sl->worker.joinable()) sl->worker.join();
+    if (sl->batch) {
+      batch_wait(sl->batch);
+      birp_batch_destroy(sl->batch);
+    }
+    delete sl;
+  }
+  for (Req* r : s->pending) delete r;
+  for (auto& kv : s->tickets)
+    if (std::find(s->pending.begin(), s->pending.end(), kv.second) == s->pending.end()) delete kv.second;
+  for (Source& src : s->sources) {
+    if (src.resident) {
+      destroy_cube_device(*src.resident);
+      delete src.resident;
+    }
+    if (src.h_vals) cudaFreeHost(src.h_vals);
+    if (src.cmem) birp_cmem_destroy(src.cmem);
+  }
+  if (s->upload_stream) {
+    cudaStreamSynchronize(s->upload_stream);
+    cudaStreamDestroy(s->upload_stream);
+  }
+  delete s;
+  return ok();
+}
+
+birp_status birp_server_add_cube(birp_server* s, const double* xs, int nx, const double* ys, int ny,
+                                 const double* zs, int nz, const float* values, int* cube_id) {
+  if (!s || !cube_id || !values || !xs || !ys || !zs) return fail(BIRP_ERR_INVALID, "NULL argument");
+  birp_cube probe;
+  const double* axes[3] = {xs, ys, zs};
+  const int n[3] = {nx, ny, nz};
+  for (int k = 0; k < 3; ++k)
+    if (birp_status rc = analyze_axis(axes[k], n[k], "xyz"[k], probe, k)) return rc;
+  Source src;
+  src.kind = 0;
+  for (int k = 0; k < 3; ++k) src.ax[k].assign(axes[k], axes[k] + n[k]);
+  size_t count = (size_t)nx * ny * nz;
+  cudaError_t e = cudaHostAlloc(&src.h_vals, count * sizeof(float), cudaHostAllocDefault);
+  if (e != cudaSuccess) return fail(BIRP_ERR_NOMEM, "pinned host copy: %s", cudaGetErrorString(e));
+  std::memcpy(src.h_vals, values, count * sizeof(float));
+  src.bytes = (int64_t)cube_device_bytes(probe);
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->sources.push_back(std::move(src));
+  *cube_id = (int)s->sources.size() - 1;
+  return ok();
+}
+
+birp_status birp_server_add_cmem(birp_server* s, const birp_cmem_params* p, int* id) {
+  if (!s || !p || !id) return fail(BIRP_ERR_INVALID, "NULL argument");
+  Source src;
+  src.kind = 1;
+  if (birp_status rc = birp_cmem_create(p, &src.cmem)) return rc;
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->sources.push_back(std::move(src));
+  *id = (int)s->sources.size() - 1;
+  return ok();
+}
+
+birp_status birp_server_submit(birp_server* s, int source_id, const birp_camera* cam, float* out_host,
+                               int64_t* ticket) {
+  if (!s || !cam || !out_host || !ticket) return fail(BIRP_ERR_INVALID, "NULL argument");
+  if (birp_status rc = validate_camera(cam)) return rc;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (source_id < 0 || source_id >= (int)s->sources.size()) return fail(BIRP_ERR_INVALID, "unknown source %d", source_id);
+  if ((int)s->pending.size() >= s->cfg.max_queue) {
+    s->st.rejected++;
+    return fail(BIRP_ERR_BUSY, "queue full (%d pending)", (int)s->pending.size());
+  }
+  Req* r = new Req();
+  r->ticket = s->next_ticket++;
+  r->src = source_id;
+  r->cam = *cam;
+  r->out = out_host;
+  r->t_submit = Clock::now();
+  s->pending.push_back(r);
+  s->tickets[r->ticket] = r;
+  s->st.submitted++;
+  *ticket = r->ticket;
+  s->cv_sched.notify_all();
+  return ok();
+}
+
+birp_status birp_server_wait(birp_server* s, int64_t ticket, double timeout_ms, birp_result* res) {
+  if (!s) return fail(BIRP_ERR_INVALID, "NULL server");
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return fail(BIRP_ERR_INVALID, "unknown ticket %lld", (long long)ticket);
+  Req* r = it->second;
+  if (timeout_ms < 0) {
+    s->cv_done.wait(lk, [&] { return r->done; });
+  } else if (!s->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), [&] { return r->done; })) {
+    return fail(BIRP_ERR_TIMEOUT, "ticket %lld not done after %.1f ms", (long long)ticket, timeout_ms);
+  }
+  if (res) {
+    res->ticket = r->ticket;
+    res->status = r->status;
+    res->latency_ms = ms_since(r->t_submit, r->t_done);
+    res->queue_ms = (r->t_launch == Clock::time_point{}) ? res->latency_ms : ms_since(r->t_submit, r->t_launch);
+  }
+  birp_status st = r->status;
+  s->tickets.erase(it);
+  delete r;
+  if (st != BIRP_OK) return fail(st, "request failed (status %d)", (int)st);
+  return ok();
+}
+
+birp_status birp_server_get_stats(const birp_server* s, birp_server_stats* out) {
+  if (!s || !out) return fail(BIRP_ERR_INVALID, "NULL argument");
+  birp_server* m = const_cast<birp_server*>(s);
+  std::lock_guard<std::mutex> lk(m->mu);
+  *out = m->st;
+  out->resident_bytes = m->resident_bytes;
+  return ok();
+}
+
+}  // extern "C"

@@ -1,0 +1,28 @@
+// Lanes-per-ray choice from the committed tuning table (tune_table.inc).
+#include <cstdint>
+
+#include "birp_host.h"
+
+namespace birp {
+
+struct TuneRow {
+  int64_t max_pixels;
+  int max_samples;
+  int kind;
+  int trilinear;
+  int seg_log2;
+};
+
+#include "tune_table.inc"
+
+int tuned_seg_log2(int64_t pixels, int n_samples, int kind, int trilinear) {
+  for (const TuneRow& r : kTuneRows) {
+    if (pixels > r.max_pixels || n_samples > r.max_samples) continue;
+    if (r.kind >= 0 && r.kind != kind) continue;
+    if (r.trilinear >= 0 && r.trilinear != (trilinear ? 1 : 0)) continue;
+    return r.seg_log2;
+  }
+  return 0;
+}
+
+}  // namespace birp

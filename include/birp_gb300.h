@@ -1,0 +1,256 @@
+/*
+ * C ABI of the GB300 BIRP render path.
+ *
+ * The render path of the reference (Zach-Clare/birp_cpp) is Camera::Render
+ * sampling a Space (a gridded DataCube or the analytic CMEM model). Each entry
+ * point below names the reference interface it replaces. Conventions:
+ *   - every call returns a birp_status; birp_last_error() gives a message
+ *     (per calling thread); no C++ exception crosses this boundary;
+ *   - handles are opaque; the caller owns the arrays it passes in and out;
+ *   - images are float, ny rows of nx, row 0 = top (as Camera::image);
+ *   - a "stream" argument is a cudaStream_t passed as void*; NULL selects the
+ *     library's own stream;
+ *   - the GPU computes in FP32 with FP64 used for the per-camera pose and for
+ *     every decision that must agree exactly with the FP64 oracle.
+ */
+#ifndef BIRP_GB300_H
+#define BIRP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  BIRP_OK = 0,
+  BIRP_ERR_INVALID = 1,   /* bad argument; reference: std::invalid_argument (src/DataCube.cpp:136) */
+  BIRP_ERR_CUDA = 2,      /* a CUDA call failed */
+  BIRP_ERR_NOMEM = 3,     /* device or pinned allocation failed, or over a memory budget */
+  BIRP_ERR_SINGULAR = 4,  /* rotation not invertible; reference: std::runtime_error (src/Helper.cpp:243) */
+  BIRP_ERR_NOT_INIT = 5,  /* birp_init not called */
+  BIRP_ERR_TIMEOUT = 6,   /* a wait ran out of time */
+  BIRP_ERR_BUSY = 7,      /* queue full */
+  BIRP_ERR_DEVICE = 8     /* a device-side consistency check failed */
+} birp_status;
+
+typedef struct birp_cube birp_cube;
+typedef struct birp_cmem birp_cmem;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int birp_version(void);
+
+/* Selects the CUDA device and creates the library's stream. No reference
+ * counterpart (the reference is CPU-only); called once before anything else. */
+birp_status birp_init(int device);
+/* Frees the library's device state. Handles must be destroyed first. */
+void birp_shutdown(void);
+/* Message of the last failing call on this thread ("" if none). */
+const char* birp_last_error(void);
+
+/* ---------------------------------------------------------------- DataCube */
+
+/* Builds a cube resident in GPU memory from axis node coordinates (strictly
+ * increasing, >= 2 nodes each) and values x-fastest:
+ * values[(k*ny + j)*nx + i] = slices[k][j][i].
+ * Replaces DataCube::Load filling coords_x/y/z, size, spacing, origin_coords
+ * and slices (src/DataCube.cpp:28-197, include/DataCube.h:30-42). Nonuniform
+ * axes are sampled with a per-cell lookup (the reference's EqualDistance check
+ * never fires, src/Helper.cpp:616, so it treats every axis as uniform). */
+birp_status birp_cube_create(const double* xs, int nx, const double* ys, int ny, const double* zs, int nz,
+                             const float* values, birp_cube** out);
+birp_status birp_cube_destroy(birp_cube* cube);
+
+typedef struct {
+  int nx, ny, nz;
+  int uniform[3];          /* 1 where the axis is uniform (affine index) */
+  size_t device_bytes;     /* GPU memory held by the cube */
+} birp_cube_info;
+birp_status birp_cube_get_info(const birp_cube* cube, birp_cube_info* info);
+
+/* Samples the cube at n points (xyz interleaved, host arrays); -1 outside the
+ * box [c0, c_{n-1}) on any axis. Replaces DataCube::GetSample
+ * (src/DataCube.cpp:203-277) with SetTrilinear (:199). */
+birp_status birp_cube_sample(const birp_cube* cube, int trilinear, const float* xyz, int n, float* out);
+
+/* ---------------------------------------------------------------- CMEM */
+
+/* The arguments of CMEM::Init (include/Cmem.h:21-41); has_v/has_b = 0 means
+ * an empty vector (defaults). 0 means "unset" for the scalar parameters, as
+ * in the reference. */
+typedef struct {
+  int has_v, v[3];
+  int has_b, b[3];
+  float dipole, p0;
+  int p1, p2, p3;
+  float B, alpha, beta, bs, A1, A2, ay_bs, az_bs, density;
+} birp_cmem_params;
+
+/* Fills the reference's default arguments (CMEM::Init() -> Init(true)). */
+void birp_cmem_default_params(birp_cmem_params* p);
+/* Runs CMEM::Init's coefficient setup on the host in FP64 (src/Cmem.cpp:38-115,
+ * 250-325, including its p2 quirk at :90) and uploads the coefficients. */
+birp_status birp_cmem_create(const birp_cmem_params* p, birp_cmem** out);
+birp_status birp_cmem_destroy(birp_cmem* cmem);
+/* CMEM::GetSample (src/Cmem.cpp:117-186) at n points on the GPU (host arrays). */
+birp_status birp_cmem_sample(const birp_cmem* cmem, const float* xyz, int n, float* out);
+
+/* ---------------------------------------------------------------- Camera */
+
+typedef enum { BIRP_MARCH_PREFIX = 0, BIRP_MARCH_CLIP = 1 } birp_march;
+
+/* What Camera holds (include/Camera.h:23-43): position, aim (only aim[0]
+ * enters the pose, as in src/Camera.cpp:92-98), field of view in degrees, with
+ * explicit image dims (the reference uses round(fov / pixel_size_deg),
+ * src/Camera.cpp:38-39), samples per ray (reference 200) and ray length in
+ * Earth radii (reference 44): sample i sits at t = (i + 0.5) * ray_length /
+ * n_samples. PREFIX stops a ray at its first out-of-box sample (the
+ * reference, src/Camera.cpp:207); CLIP integrates every in-box sample.
+ * segments: lanes per ray (1, 2, 4, 8), 0 = tuned choice. */
+typedef struct {
+  double pos[3];
+  double aim[3];
+  double fov_w_deg, fov_h_deg;
+  int nx, ny;
+  int n_samples;
+  double ray_length;
+  int trilinear;
+  int march;
+  int segments;
+} birp_camera;
+
+/* Fills the reference's CLI defaults (src/main.cpp:37-63): pos
+ * (5.91813, 6.74116, 17.7067), aim (7.81768, 0, 0), 36 x 36 degrees at 0.25
+ * degree pixels (144 x 144), 200 samples over 44 Re, nearest, PREFIX. */
+void birp_camera_defaults(birp_camera* cam);
+
+/* Renders one image of a cube (cmem == NULL) or of CMEM (cube == NULL) into a
+ * HOST array of ny*nx floats; returns when the image is in out_host.
+ * Replaces Camera::Render (src/Camera.cpp:63-233) — except that the output is
+ * overwritten, where the reference adds to Camera::image. */
+birp_status birp_render(const birp_cube* cube, const birp_cmem* cmem, const birp_camera* cam, float* out_host,
+                        void* stream);
+/* Same, into DEVICE memory, asynchronous on the stream. */
+birp_status birp_render_device(const birp_cube* cube, const birp_cmem* cmem, const birp_camera* cam,
+                               float* out_device, void* stream);
+
+/* The FP64 frame of a camera as the kernels use it: R^-1 (row-major 9),
+ * tan(fov_w/2), tan(fov_h/2), aspect nx/ny, step, per-sample scale
+ * (src/Camera.cpp:201) and the Sun roll angle of Camera::Orient
+ * (src/Camera.cpp:309-417), all FP64. */
+birp_status birp_camera_frame(const birp_camera* cam, double* rinv9, double* tan_w, double* tan_h,
+                              double* aspect, double* step, double* scale, double* angle_sun);
+
+/* ---------------------------------------------------------------- batches */
+
+/* A batch renders many requests (any mix of cubes, CMEM, image sizes, steps)
+ * in ONE launch of a persistent kernel, replayed from a CUDA graph. Replaces
+ * the reference's one-render-per-cube loop (src/main.cpp:242-264). */
+typedef struct {
+  const birp_cube* cube;   /* exactly one of cube / cmem */
+  const birp_cmem* cmem;
+  birp_camera cam;
+} birp_request;
+
+typedef struct birp_batch birp_batch;
+
+/* max_requests and max_pixels bound one launch; the batch owns device and
+ * pinned host buffers of that size. */
+birp_status birp_batch_create(int max_requests, int64_t max_pixels, birp_batch** out);
+birp_status birp_batch_destroy(birp_batch* b);
+/* Starts rendering n requests on the batch's stream and returns. */
+birp_status birp_batch_submit(birp_batch* b, const birp_request* reqs, int n);
+/* Waits for the submitted requests; images land in the batch's pinned host
+ * buffer (birp_batch_image). */
+birp_status birp_batch_wait(birp_batch* b);
+/* Pointer to request i's image in the pinned host buffer, valid until the
+ * next submit. */
+const float* birp_batch_image(const birp_batch* b, int i);
+/* submit + wait + copy each image to outs[i] (host arrays of ny*nx floats). */
+birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, float* const* outs);
+/* Device time of the batch's last launch in ms (CUDA events around the
+ * graph: H2D of descriptors, kernel, D2H of the images). */
+birp_status birp_batch_last_ms(const birp_batch* b, float* kernel_ms, float* total_ms);
+
+/* ---------------------------------------------------------------- serving */
+
+/* A continuous-batching server: requests are admitted as they arrive; a
+ * scheduler thread groups pending requests into batches, launches them on
+ * `slots` concurrent streams as slots and cube memory free up, and keeps
+ * cubes resident in GPU memory under a byte budget with LRU eviction and
+ * re-upload from host (pinned) copies. */
+typedef struct birp_server birp_server;
+
+typedef struct {
+  int64_t cube_budget_bytes;   /* GPU bytes the resident cubes may hold */
+  int slots;                   /* batches in flight */
+  int max_batch_requests;
+  int64_t max_batch_pixels;
+  int max_queue;               /* pending requests before submit returns BIRP_ERR_BUSY */
+  double max_wait_ms;          /* batching window: launch when this old or the batch is full */
+} birp_server_config;
+
+typedef struct {
+  int64_t ticket;
+  birp_status status;
+  double latency_ms;           /* submit -> image in host memory */
+  double queue_ms;             /* submit -> launch */
+} birp_result;
+
+typedef struct {
+  int64_t submitted, completed, rejected, batches;
+  int64_t cube_uploads, cube_evictions, cube_hits;
+  int64_t resident_bytes;
+} birp_server_stats;
+
+void birp_server_default_config(birp_server_config* c);
+birp_status birp_server_create(const birp_server_config* c, birp_server** out);
+birp_status birp_server_destroy(birp_server* s);
+/* Registers a cube whose values stay in HOST memory (copied into pinned
+ * memory); it is uploaded on first use and may be evicted. */
+birp_status birp_server_add_cube(birp_server* s, const double* xs, int nx, const double* ys, int ny,
+                                 const double* zs, int nz, const float* values, int* cube_id);
+birp_status birp_server_add_cmem(birp_server* s, const birp_cmem_params* p, int* source_id);
+/* Queues one render of source_id; the image is written to out_host
+ * (ny*nx floats) before the ticket completes. */
+birp_status birp_server_submit(birp_server* s, int source_id, const birp_camera* cam, float* out_host,
+                               int64_t* ticket);
+/* Waits for a ticket (timeout_ms < 0: no limit). */
+birp_status birp_server_wait(birp_server* s, int64_t ticket, double timeout_ms, birp_result* res);
+birp_status birp_server_get_stats(const birp_server* s, birp_server_stats* st);
+
+/* ---------------------------------------------------------------- telemetry */
+
+typedef struct {
+  uint64_t exact_range_rays;   /* rays whose in-box range was decided in FP64 */
+  uint64_t exact_nearest;      /* nearest-mode samples decided in FP64 */
+  uint64_t exact_cmem;         /* CMEM samples decided in FP64 */
+  uint64_t items;              /* tiles rendered by the persistent kernel */
+  uint64_t samples;            /* ray-samples evaluated (the roofline's unit) */
+} birp_kernel_stats;
+
+/* Reads (and optionally clears) the kernels' counters. */
+birp_status birp_get_kernel_stats(birp_kernel_stats* st, int reset);
+
+/* Timing of one plain render on the library stream with CUDA events: the
+ * render kernel alone (kernel_ms) — used by the benchmark for the roofline. */
+birp_status birp_time_render_device(const birp_cube* cube, const birp_cmem* cmem, const birp_camera* cam,
+                                    float* out_device, int repeats, int flush_l2, float* kernel_ms);
+
+/* Writes a 512 MB buffer (larger than L2) on the library stream and waits:
+ * run between timed renders so each starts with a cold L2. */
+birp_status birp_flush_l2(void);
+
+/* Roofline denominators measured on this GPU: FP32 FMA throughput (TFLOP/s,
+ * FMA = 2 flops) and the read bandwidth of an L2-resident buffer (GB/s). */
+birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs);
+
+/* Largest FP32 relative error of the CMEM boundary radii against FP64 over n
+ * directions (a self-check of the margin the kernels use). */
+birp_status birp_cmem_margin_check(const birp_cmem* cmem, int n, float* max_rel_err, float* margin);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BIRP_GB300_H */

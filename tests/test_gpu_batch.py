@@ -1,0 +1,148 @@
+"""The batched path (one persistent-kernel launch from a CUDA graph) and the
+continuous-batching server give the same images as the plain per-call render,
+bit for bit, alone and in a mix."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def spaces(birp):
+    from birp_cpp_gb300 import synth
+    xs, ys, zs, v = synth.cube_config1(seed=1, n=96)
+    c1 = birp.Cube(xs, ys, zs, v.astype(np.float32))
+    xs0, ys0, zs0, v0 = synth.cube_config0(seed=0)
+    c0 = birp.Cube(xs0, ys0, zs0, v0.astype(np.float32))
+    return dict(c1=c1, c0=c0, cmem=birp.Cmem(), host=dict(c1=(xs, ys, zs, v.astype(np.float32)),
+                                                          c0=(xs0, ys0, zs0, v0.astype(np.float32))))
+
+
+def mixed_items(birp, spaces, n=24, seed=9):
+    from birp_cpp_gb300 import synth
+    rng = np.random.default_rng(seed)
+    reqs = synth.config2_requests(n, seed=seed)
+    items = []
+    for k, (pos, aim, nx, ny, step) in enumerate(reqs):
+        nx, ny = max(8, nx // 8), max(6, ny // 8)
+        kind = rng.integers(0, 4)
+        space = [spaces["c1"], spaces["c1"], spaces["c0"], spaces["cmem"]][kind]
+        cam = birp.camera(pos, aim, 27.0, 16.0, nx, ny, n_samples=synth.n_samples(step),
+                          trilinear=bool(rng.integers(0, 2)), march=int(rng.integers(0, 2)))
+        items.append((space, cam))
+    return items
+
+
+def test_batch_equals_plain_bitwise(birp, spaces):
+    items = mixed_items(birp, spaces)
+    b = birp.Batch(64, 1 << 22)
+    outs = b.render(items)
+    for (space, cam), img in zip(items, outs):
+        ref = birp.render(space, cam)
+        assert np.array_equal(img, ref)
+    kms, tms = b.last_ms()
+    assert 0 < kms <= tms
+    # a second launch of the same graph with other requests
+    items2 = mixed_items(birp, spaces, n=7, seed=3)
+    outs2 = b.render(items2)
+    for (space, cam), img in zip(items2, outs2):
+        assert np.array_equal(img, birp.render(space, cam))
+    b.close()
+
+
+def test_batch_single_and_empty(birp, spaces):
+    b = birp.Batch(4, 1 << 16)
+    cam = birp.camera((3, 1, 2), (9, 0, 0), 27.0, 16.0, 40, 24, n_samples=440)
+    [img] = b.render([(spaces["c1"], cam)])
+    assert np.array_equal(img, birp.render(spaces["c1"], cam))
+    assert b.render([]) == []
+    with pytest.raises(birp.BirpError):
+        b.render([(spaces["c1"], birp.camera((3, 1, 2), (9, 0, 0), 27.0, 16.0, 400, 240))])  # > max_pixels
+    b.close()
+
+
+def test_server_same_alone_and_in_mix(birp, spaces):
+    """Each request's image from the server equals its plain render, whether
+    it ran alone or mixed with others arriving concurrently."""
+    srv = birp.Server(birp.server_config(slots=3, max_batch_requests=16, max_batch_pixels=1 << 20,
+                                         max_wait_ms=0.5))
+    ids = {"c1": srv.add_cube(*spaces["host"]["c1"]), "c0": srv.add_cube(*spaces["host"]["c0"]),
+           "cmem": srv.add_cmem()}
+    name_of = {id(spaces["c1"]): "c1", id(spaces["c0"]): "c0", id(spaces["cmem"]): "cmem"}
+    items = mixed_items(birp, spaces, n=40, seed=21)
+    # alone
+    space, cam = items[0]
+    out = np.empty((cam.ny, cam.nx), np.float32)
+    t = srv.submit(ids[name_of[id(space)]], cam, out)
+    r = srv.wait(t)
+    assert r.status == 0 and r.latency_ms > 0
+    assert np.array_equal(out, birp.render(space, cam))
+    # in a mix: all submitted at once and in bursts
+    outs, tickets = [], []
+    for k, (space, cam) in enumerate(items):
+        o = np.empty((cam.ny, cam.nx), np.float32)
+        outs.append(o)
+        tickets.append(srv.submit(ids[name_of[id(space)]], cam, o))
+        if k % 10 == 9:
+            time.sleep(0.002)
+    for t in tickets:
+        assert srv.wait(t, 30000).status == 0
+    for (space, cam), o in zip(items, outs):
+        assert np.array_equal(o, birp.render(space, cam))
+    st = srv.stats()
+    assert st.completed == len(items) + 1 and st.batches >= 2
+    srv.close()
+
+
+def test_server_lru_eviction_and_errors(birp, spaces):
+    from birp_cpp_gb300 import synth
+    cubes = []
+    for s in range(3):
+        xs, ys, zs, v = synth.cube_config1(seed=40 + s, n=64)
+        cubes.append((xs, ys, zs, v.astype(np.float32)))
+    one = birp.Cube(*cubes[0]).info().device_bytes
+    # budget for two cubes: cycling through three forces evictions + re-uploads
+    srv = birp.Server(birp.server_config(cube_budget_bytes=int(2.5 * one), slots=2, max_batch_requests=4,
+                                         max_batch_pixels=1 << 18, max_wait_ms=0.0))
+    ids = [srv.add_cube(*c) for c in cubes]
+    gpu_cubes = [birp.Cube(*c) for c in cubes]
+    cam = birp.camera((2, -3, 4), (9, 0, 0), 27.0, 16.0, 48, 28, n_samples=440)
+    for rnd in range(3):
+        for k in (0, 1, 2):
+            o = np.empty((28, 48), np.float32)
+            t = srv.submit(ids[k], cam, o)
+            assert srv.wait(t, 30000).status == 0
+            assert np.array_equal(o, birp.render(gpu_cubes[k], cam))
+    st = srv.stats()
+    assert st.cube_evictions >= 3 and st.cube_uploads >= 4
+    assert st.resident_bytes <= int(2.5 * one)
+    srv.close()
+    # a cube larger than the budget fails cleanly with NOMEM
+    srv = birp.Server(birp.server_config(cube_budget_bytes=1000, slots=1))
+    cid = srv.add_cube(*cubes[0])
+    o = np.empty((28, 48), np.float32)
+    t = srv.submit(cid, cam, o)
+    r = srv.wait(t, 30000)
+    assert r.status == birp.ERR_NOMEM
+    srv.close()
+    # a full queue rejects with BUSY; a short wait times out without harm
+    srv = birp.Server(birp.server_config(max_queue=1, slots=1, max_wait_ms=0.0))
+    cid = srv.add_cmem()
+    big = birp.camera((2, -3, 4), (9, 0, 0), 27.0, 16.0, 512, 300, n_samples=1760)
+    outs = [np.empty((300, 512), np.float32) for _ in range(6)]
+    tickets, busy = [], 0
+    for o in outs:
+        try:
+            tickets.append(srv.submit(cid, big, o))
+        except birp.BirpError as e:
+            assert e.status == birp.ERR_BUSY
+            busy += 1
+    assert busy >= 1
+    with pytest.raises(birp.BirpError) as e:
+        srv.wait(tickets[-1], 0.0)
+    assert e.value.status == birp.ERR_TIMEOUT
+    for t in tickets:
+        assert srv.wait(t, 60000).status == 0
+    srv.close()
