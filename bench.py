@@ -387,7 +387,9 @@ def serve_latency(B, W, rate: float, seconds: float, seed: int = 13):
     reqs = synth.config2_requests(4096, seed=seed)
     rng = np.random.default_rng(seed)
     cams = [B.camera(p, a, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(s)) for p, a, nx, ny, s in reqs]
-    bufs = [np.empty((c.ny, c.nx), np.float32) for c in cams[:256]]
+    # one buffer per in-flight request slot, each large enough for any image
+    max_px = max(c.nx * c.ny for c in cams)
+    bufs = [np.empty(max_px, np.float32) for _ in range(256)]
     # warm the cube into GPU memory
     t = srv.submit(sid, cams[0], bufs[0])
     srv.wait(t)

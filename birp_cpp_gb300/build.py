@@ -17,6 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libbirp_gb300.so")
+CLASSES_LIB = os.path.join(LIBDIR, "libbirp_classes.so")
+CPP = os.path.join(HERE, "cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["render.cu", "capi.cu", "cube.cu", "batch.cu", "server.cu", "cmem_host.cpp", "tune.cpp"]
@@ -60,9 +62,24 @@ def build(verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    build_classes()
     if verbose:
-        print("built", LIB)
+        print("built", LIB, "and", CLASSES_LIB)
     return LIB
+
+
+def build_classes() -> str:
+    """The reference-API C++ classes (cpp/) over the C ABI: libbirp_classes.so."""
+    src = os.path.join(CPP, "src", "classes.cpp")
+    deps = [src, LIB] + [os.path.join(CPP, "include", "birp", h) for h in os.listdir(os.path.join(CPP, "include", "birp"))]
+    if os.path.exists(CLASSES_LIB) and all(os.path.getmtime(CLASSES_LIB) >= os.path.getmtime(d) for d in deps):
+        return CLASSES_LIB
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", src, "-I", os.path.join(CPP, "include"),
+           "-L", LIBDIR, "-lbirp_gb300", "-Wl,-rpath,$ORIGIN", "-o", CLASSES_LIB]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"classes build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return CLASSES_LIB
 
 
 if __name__ == "__main__":

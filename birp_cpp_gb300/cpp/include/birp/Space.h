@@ -1,0 +1,20 @@
+// Drop-in for the reference's Space interface (include/Space.h:18-23): the
+// abstract emissivity field a Camera samples. The two pure virtuals keep the
+// reference's signatures; the GPU handles let Camera::Render launch the
+// fused GB300 kernels instead of calling GetSample per sample.
+#pragma once
+
+struct birp_cube;
+struct birp_cmem;
+
+class Space {
+ public:
+  virtual ~Space() = default;
+  virtual void Init() = 0;
+  virtual float GetSample(float x, float y, float z) = 0;
+  // GPU representation (exactly one is non-null for the built-in spaces). A
+  // user-defined Space without one cannot be rendered: there is no CPU path.
+  virtual const birp_cube* GpuCube() { return nullptr; }
+  virtual const birp_cmem* GpuCmem() { return nullptr; }
+  virtual bool Trilinear() const { return false; }
+};

@@ -97,8 +97,8 @@ void cmem_coefficients(const birp_cmem_params& g, CmemDev& m) {
   m.d_bc0 = bc0;
   m.d_bc1 = bc1;
   m.d_bc3 = bc3;
-  // FP32 radii of the shell surfaces agree with FP64 to ~1e-6 relative
-  // (checked by birp_cmem_margin_check); decide in FP64 within 2e-5.
+  // FP32 radii of the shell surfaces agree with FP64 to ~1e-6 of (r + 5 Re)
+  // (checked by birp_cmem_margin_check); decide in FP64 within 2e-5 of it.
   m.eps_rel = 2e-5f;
 }
 

@@ -182,30 +182,58 @@ struct CmemEval {
 };
 
 // CMEM::GetSample in FP32 (src/Cmem.cpp:117-186 with ShueCoords :224-246,
-// LinScaled :188-222, ShueModel :280-288). cos(phi - pi/2) = sin(phi) and
-// cos(phi - 3pi/2) = -sin(phi). `unsure` flags samples whose shell choice
-// lies within the FP32 error bound of a discontinuous shell edge.
-__device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
-  float r = sqrtf(x * x + y * y + z * z);
-  float theta = (x != 0.f) ? acosf(x / r) : 0.f;
-  float phi = (y != 0.f) ? acosf(y / sqrtf(y * y + z * z)) : 0.f;
-  float st, ct, sp, cp;
+// LinScaled :188-222, ShueModel :280-288), rewritten in forms that stay
+// well conditioned in FP32 (the same values in exact arithmetic):
+//   theta = acos(x/r)           -> atan2(sqrt(y^2+z^2), x)
+//   phi   = acos(y/sqrt(y^2+z^2)) -> atan2(|z|, y)
+//   phi_n = acos(u . n_N)       -> atan2(|u x n_N|, u . n_N), with the unit
+//           direction u = (cos t, sin t cos p, sin t sin p) and the cusp axis
+//           n_N = (cos t_n, 0, sin t_n) (cos(p - pi/2) = sin p); n_S likewise
+//           with -sin t_s (cos(p - 3pi/2) = -sin p)
+//   2 / (1 + cos t)             -> 1 / cos^2(t/2)
+// and the reference's quirks kept: theta = 0 when x == 0, phi = 0 when y == 0.
+// `unsure` flags samples whose shell choice lies within the FP32 error bound
+// (eps_rel * (r + 5 Re): relative with an absolute floor for the small radii
+// where the Lin model cancels, plus the position error perr) of a
+// discontinuous edge.
+__device__ __forceinline__ void cmem_angles32(float x, float y, float z, float& r, float& theta, float& phi) {
+  float ryz = sqrtf(y * y + z * z);
+  r = sqrtf(x * x + y * y + z * z);
+  theta = (x != 0.f) ? atan2f(ryz, x) : 0.f;
+  phi = (y != 0.f) ? atan2f(fabsf(z), y) : 0.f;
+}
+
+__device__ __forceinline__ void cmem_radii32(const CmemDev& m, float theta, float phi, float& r_mp, float& r_bs,
+                                             float& st, float& ct, float& sp, float& cp) {
   sincosf(theta, &st, &ct);
   sincosf(phi, &sp, &cp);
-  float phi_n = acosf(ct * m.cos_tn + st * m.sin_tn * sp);
-  float phi_s = acosf(ct * m.cos_ts - st * m.sin_ts * sp);
-  float base = cosf(0.5f * theta) + m.a5 * (2.f * st * ct) * (1.f - expf(-theta));
+  // angle to the northern / southern cusp axes
+  const float ux = ct, uy = st * cp, uz = st * sp;
+  float dn = ux * m.cos_tn + uz * m.sin_tn;
+  float cnx = uy * m.sin_tn, cny = uz * m.cos_tn - ux * m.sin_tn, cnz = -uy * m.cos_tn;
+  float phi_n = atan2f(sqrtf(cnx * cnx + cny * cny + cnz * cnz), dn);
+  float ds = ux * m.cos_ts - uz * m.sin_ts;
+  float csx = -uy * m.sin_ts, csy = uz * m.cos_ts + ux * m.sin_ts, csz = -uy * m.cos_ts;
+  float phi_s = atan2f(sqrtf(csx * csx + csy * csy + csz * csz), ds);
+  float ch = cosf(0.5f * theta);
+  float base = ch + m.a5 * (2.f * st * ct) * (1.f - expf(-theta));
   float f = powf(base, m.p1 * (m.bc0 + m.bc1 * cp + m.bc3 * (sp * sp)));
   float q = m.p2c * expf(m.p3dn * powf(phi_n, m.a21)) + m.p2c * expf(m.p3ds * powf(phi_s, m.a21));
-  float r_mp = m.p0r0 * f + q;
-  float b2 = 2.f / (1.f + ct);
+  r_mp = m.p0r0 * f + q;
+  float b2 = 1.f / (ch * ch);
   float ry = m.bs * powf(b2, m.ay);
   float rz = m.bs * powf(b2, m.az);
   float a1 = rz * cp, a2 = ry * sp;
-  float r_bs = (ry * rz) / sqrtf(a1 * a1 + a2 * a2);
+  r_bs = (ry * rz) / sqrtf(a1 * a1 + a2 * a2);
+}
+
+__device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
+  float r, theta, phi, r_mp, r_bs, st, ct, sp, cp;
+  cmem_angles32(x, y, z, r, theta, phi);
+  cmem_radii32(m, theta, phi, r_mp, r_bs, st, ct, sp, cp);
   const float half = 0.025f;
   CmemEval out;
-  float tol = fmaf(m.eps_rel, r, perr);
+  float tol = fmaf(m.eps_rel, r + 5.f, perr);
   out.unsure = !(fabsf(r - (r_mp + half)) > tol) || !(fabsf(r - (r_bs + half)) > tol);
   float h = 0.5f * theta;
   float h4 = (h * h) * (h * h);
@@ -677,23 +705,9 @@ __global__ void cmem_sample_kernel(const CmemDev* __restrict__ cmem, const float
 }
 
 // Validates the FP32 CMEM boundary-radius error bound: max over n pseudo-
-// random directions of |r32 - r64| / r64 for both surfaces.
-__device__ void cmem_radii32(const CmemDev& m, float theta, float phi, float& r_mp, float& r_bs) {
-  float st, ct, sp, cp;
-  sincosf(theta, &st, &ct);
-  sincosf(phi, &sp, &cp);
-  float phi_n = acosf(ct * m.cos_tn + st * m.sin_tn * sp);
-  float phi_s = acosf(ct * m.cos_ts - st * m.sin_ts * sp);
-  float base = cosf(0.5f * theta) + m.a5 * (2.f * st * ct) * (1.f - expf(-theta));
-  float f = powf(base, m.p1 * (m.bc0 + m.bc1 * cp + m.bc3 * (sp * sp)));
-  float q = m.p2c * expf(m.p3dn * powf(phi_n, m.a21)) + m.p2c * expf(m.p3ds * powf(phi_s, m.a21));
-  r_mp = m.p0r0 * f + q;
-  float b2 = 2.f / (1.f + ct);
-  float ry = m.bs * powf(b2, m.ay), rz = m.bs * powf(b2, m.az);
-  float a1 = rz * cp, a2 = ry * sp;
-  r_bs = (ry * rz) / sqrtf(a1 * a1 + a2 * a2);
-}
-
+// random directions of |r32 - r64| / (|r64| + 5 Re), over the surfaces closer
+// than 100 Re (farther ones are out of reach of the rays, so no shell
+// decision depends on them).
 __global__ void cmem_radii_check_kernel(const CmemDev* __restrict__ cmem, int n, unsigned long long seed,
                                         float* max_err) {
   const CmemDev& m = *cmem;
@@ -706,8 +720,8 @@ __global__ void cmem_radii_check_kernel(const CmemDev* __restrict__ cmem, int n,
     h ^= h >> 32;
     float theta = (float)((h & 0xFFFFFF) * (pi * 0.999 / 16777216.0));
     float phi = (float)(((h >> 24) & 0xFFFFFF) * (pi / 16777216.0));
-    float r_mp, r_bs;
-    cmem_radii32(m, theta, phi, r_mp, r_bs);
+    float r_mp, r_bs, st32, ct32, sp32, cp32;
+    cmem_radii32(m, theta, phi, r_mp, r_bs, st32, ct32, sp32, cp32);
     double th = theta, ph = phi;
     double phi_n = acos(cos(th) * cos(m.d_tn) + sin(th) * sin(m.d_tn) * cos(ph - pi / 2));
     double phi_s = acos(cos(th) * cos(m.d_ts) + sin(th) * sin(m.d_ts) * cos(ph - 3 * pi / 2));
@@ -721,10 +735,10 @@ __global__ void cmem_radii_check_kernel(const CmemDev* __restrict__ cmem, int n,
     double ry = m.d_bs * pow(bb, m.d_ay), rz = m.d_bs * pow(bb, m.d_az);
     double a1 = rz * cos(ph), a2 = ry * sin(ph);
     double bs64 = (ry * rz) / sqrt(a1 * a1 + a2 * a2);
-    float e1 = (float)(fabs((double)r_mp - mp64) / mp64);
-    float e2 = (float)(fabs((double)r_bs - bs64) / bs64);
-    if (isfinite(e1)) worst = fmaxf(worst, e1);
-    if (isfinite(e2)) worst = fmaxf(worst, e2);
+    float e1 = (float)(fabs((double)r_mp - mp64) / (fabs(mp64) + 5.0));
+    float e2 = (float)(fabs((double)r_bs - bs64) / (fabs(bs64) + 5.0));
+    if (isfinite(e1) && fabs(mp64) < 100.0) worst = fmaxf(worst, e1);
+    if (isfinite(e2) && bs64 < 100.0) worst = fmaxf(worst, e2);
   }
   // non-negative floats order like their bit patterns
   atomicMax(reinterpret_cast<unsigned int*>(max_err), __float_as_uint(worst));

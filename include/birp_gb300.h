@@ -246,8 +246,9 @@ birp_status birp_flush_l2(void);
  * FMA = 2 flops) and the read bandwidth of an L2-resident buffer (GB/s). */
 birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs);
 
-/* Largest FP32 relative error of the CMEM boundary radii against FP64 over n
- * directions (a self-check of the margin the kernels use). */
+/* Largest FP32 error of the CMEM boundary radii against FP64 over n
+ * directions, relative to (|r| + 5 Re), where the radius is under 100 Re (a
+ * self-check of the margin the kernels use; margin receives that margin). */
 birp_status birp_cmem_margin_check(const birp_cmem* cmem, int n, float* max_rel_err, float* margin);
 
 #ifdef __cplusplus

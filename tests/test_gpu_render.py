@@ -176,15 +176,22 @@ def test_cmem_sample_kats(birp, golden):
         assert np.allclose(got, want, rtol=2e-6, atol=0), (name, got, want)
 
 
-def test_cmem_samples_vs_reference(birp, golden):
-    """3000 CMEM points against the reference's FP32 GetSample."""
+def test_cmem_samples_vs_oracle(birp, oracle, golden):
+    """3000 CMEM points against the FP64 oracle. Shell choices are exact
+    (zero vs non-zero agree); values agree to 1e-5 except inside the 0.05 Re
+    ramp shells, where the value is proportional to r - r_mp and inherits the
+    FP32 error of r_mp (~1e-5 Re absolute), so the bound there is absolute."""
     pts = golden["cmem"]["points"]
-    got = birp.Cmem().sample(pts)
-    want = golden["cmem"]["default"]
-    m = want > 0
-    assert np.array_equal(got == 0, want == 0)
-    r = np.abs(got[m] - want[m]) / want[m]
-    assert np.quantile(r, 0.999) < 1e-5
+    got = birp.Cmem().sample(pts).astype(np.float64)
+    ref = oracle.Cmem64().sample(pts.astype(np.float64))
+    assert np.array_equal(got == 0, ref == 0)
+    m = ref > 0
+    r = np.abs(got[m] - ref[m]) / ref[m]
+    assert np.quantile(r, 0.999) < 1e-5, np.quantile(r, 0.999)
+    assert np.abs(got - ref).max() < 1e-5 * ref.max()
+    # and the reference's FP32 values are within their own accuracy of both
+    want = golden["cmem"]["default"].astype(np.float64)
+    assert np.quantile(np.abs(want[m] - ref[m]) / ref[m], 0.99) < 1e-5
 
 
 def test_cube_sample_matches_oracle(birp, oracle, golden, cube1):
