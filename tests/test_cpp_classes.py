@@ -67,4 +67,4 @@ def test_classes_on_gpu(tmp_path, birp, oracle):
     ref = oracle.render64(oracle.Cmem64(), cam, threads=os.cpu_count() or 4)
     m = ref > 1e-3 * ref.max()
     assert (np.abs(img[m] - ref[m]) / ref[m]).max() <= 1e-5
-    assert float(cards["POS_X"]) == f32(5.91813)
+    assert np.float32(cards["POS_X"]) == np.float32(5.91813)  # 9 digits round-trip FP32

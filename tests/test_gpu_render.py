@@ -178,16 +178,29 @@ def test_cmem_sample_kats(birp, golden):
 
 def test_cmem_samples_vs_oracle(birp, oracle, golden):
     """3000 CMEM points against the FP64 oracle. Shell choices are exact
-    (zero vs non-zero agree); values agree to 1e-5 except inside the 0.05 Re
-    ramp shells, where the value is proportional to r - r_mp and inherits the
-    FP32 error of r_mp (~1e-5 Re absolute), so the bound there is absolute."""
+    (zero vs non-zero agree). Values agree to 1e-5 relative outside the
+    0.05 Re ramp shells; inside them the value is proportional to r - r_mp and
+    inherits the FP32 error of r_mp (~1e-5 Re), so there the bound is on the
+    absolute error (it moves a ray sum by < 1e-8 of itself)."""
+    import ctypes as C
     pts = golden["cmem"]["points"]
     got = birp.Cmem().sample(pts).astype(np.float64)
-    ref = oracle.Cmem64().sample(pts.astype(np.float64))
+    om = oracle.Cmem64()
+    p64 = pts.astype(np.float64)
+    ref = om.sample(p64)
     assert np.array_equal(got == 0, ref == 0)
-    m = ref > 0
-    r = np.abs(got[m] - ref[m]) / ref[m]
-    assert np.quantile(r, 0.999) < 1e-5, np.quantile(r, 0.999)
+    x, y, z = p64.T
+    r = np.sqrt(x * x + y * y + z * z)
+    ramp = np.zeros(len(pts), bool)
+    for k in range(len(pts)):
+        th = np.arccos(x[k] / r[k]) if x[k] != 0 else 0.0
+        ph = np.arccos(y[k] / np.hypot(y[k], z[k])) if y[k] != 0 else 0.0
+        a, b = C.c_double(), C.c_double()
+        oracle.lib().oracle_cmem64_radii(C.byref(om.s), th, ph, C.byref(a), C.byref(b))
+        ramp[k] = abs(r[k] - a.value) <= 0.0251 or abs(r[k] - b.value) <= 0.0251
+    m = (ref > 0) & ~ramp
+    rel = np.abs(got[m] - ref[m]) / ref[m]
+    assert rel.max() < 1e-5, rel.max()
     assert np.abs(got - ref).max() < 1e-5 * ref.max()
     # and the reference's FP32 values are within their own accuracy of both
     want = golden["cmem"]["default"].astype(np.float64)
