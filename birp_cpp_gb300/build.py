@@ -21,7 +21,7 @@ CLASSES_LIB = os.path.join(LIBDIR, "libbirp_classes.so")
 CPP = os.path.join(HERE, "cpp")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["render.cu", "capi.cu", "cube.cu", "batch.cu", "server.cu", "cmem_host.cpp", "tune.cpp"]
+SOURCES = ["render.cu", "capi.cu", "cube.cu", "batch.cu", "server.cu", "noalloc.cu", "cmem_host.cpp", "tune.cpp"]
 
 
 def nvcc() -> str:

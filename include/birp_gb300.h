@@ -169,6 +169,20 @@ birp_status birp_batch_wait(birp_batch* b);
 const float* birp_batch_image(const birp_batch* b, int i);
 /* submit + wait + copy each image to outs[i] (host arrays of ny*nx floats). */
 birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, float* const* outs);
+/* Renders n requests (n <= 256) like birp_batch_submit but allocates nothing,
+ * for callers that cannot call cudaMalloc on their render path (code running
+ * inside another framework's operator, where that framework owns the device
+ * memory; loops that must not allocate). The caller passes the requests and
+ * one DEVICE output buffer of ny*nx floats per request; the only other device
+ * memory used is a 64 KB array inside this library (held on every GPU that
+ * loads it), set up by the first call on each device (make that first call
+ * before any stream capture). Asynchronous on `stream` (NULL: the library's
+ * stream if initialised on this device, else the default stream). Every call
+ * shares that array, so calls whose work overlaps on the GPU race: order them
+ * on one stream. More than 256 requests is BIRP_ERR_INVALID. No counterpart in
+ * the reference. */
+birp_status birp_batch_render_noalloc(const birp_request* reqs, int n, float* const* outs_device, void* stream);
+
 /* Device time of the batch's last launch in ms (CUDA events around the
  * graph: H2D of descriptors, kernel, D2H of the images). */
 birp_status birp_batch_last_ms(const birp_batch* b, float* kernel_ms, float* total_ms);
