@@ -293,6 +293,29 @@ def main():
         plain_s = allreduce_max(world, min(pt))
         plain = world * args.requests / plain_s
 
+    # ---- batched vs plain per image size (each class alone)
+    by_size = None
+    if not args.no_plain and rank == 0:
+        by_size = {}
+        img_buf = np.empty(max(c.nx * c.ny for c in cams), np.float32)
+        for sz in sorted({(c.nx, c.ny) for c in cams}):
+            sel = [c for c in cams if (c.nx, c.ny) == sz]
+            its = [(cube, c) for c in sel]
+            tb, tp = [], []
+            for rep in range(2):
+                B.flush_l2()
+                batch.submit(its)
+                batch.wait()
+                tb.append(batch.last_ms()[0])
+                B.flush_l2()
+                t0 = time.perf_counter()
+                for c in sel:
+                    B.render(cube, c, out=img_buf[: c.nx * c.ny].reshape(c.ny, c.nx))
+                tp.append(1000 * (time.perf_counter() - t0))
+            bi, pi = len(sel) / (min(tb) / 1000), len(sel) / (min(tp) / 1000)
+            by_size[f"{sz[0]}x{sz[1]}"] = {"requests": len(sel), "batched_images_s": bi, "plain_images_s": pi,
+                                          "batched_vs_plain": bi / pi}
+
     # ---- roofline of the batched kernel (measured peaks)
     fp32_tflops, l2_gbs = B.measure_peaks()
     t_k = step_ms / 1000.0
@@ -341,6 +364,7 @@ def main():
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 4 * total_px},
             "plain": {"value": plain, "unit": UNIT} if plain else None,
             "batched_vs_plain": (value / plain) if plain else None,
+            "by_size": by_size,
             "e2e_vs_plain": (e2e / plain) if plain else None,
             "serving": serving,
             "ray_samples_per_s": samples_per_step * world / (step_ms / 1000.0),

@@ -26,8 +26,10 @@ static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 static void free_batch(birp_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
+  for (int c = 0; c < 2; ++c) {
+    if (b->exec[c]) cudaGraphExecDestroy(b->exec[c]);
+    if (b->graph[c]) cudaGraphDestroy(b->graph[c]);
+  }
   if (b->h_stage) cudaFreeHost(b->h_stage);
   if (b->h_out) cudaFreeHost(b->h_out);
   if (b->d_stage) cudaFree(b->d_stage);
@@ -76,18 +78,19 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   bd.reqs = reinterpret_cast<const RequestDev*>(b->d_stage + b->off_reqs);
   bd.counter = b->d_counter;
   bd.stats = g_ctx.stats;
-  b->grid = persistent_grid(0);
-
-  // capture: descriptors H2D, queue head reset, persistent kernel
-  if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-    return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
-  cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
-  cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), b->stream);
-  launch_render_batch(bd, b->grid, b->stream);
-  e = cudaStreamEndCapture(b->stream, &b->graph);
-  if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
-  if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess)
-    return bail(fail(BIRP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  // capture per kernel class: descriptors H2D, queue head reset, persistent kernel
+  for (int cls = 0; cls < 2; ++cls) {
+    b->grid[cls] = persistent_grid(cls);
+    if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+      return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+    cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
+    cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), b->stream);
+    launch_render_batch(bd, b->grid[cls], b->stream, cls);
+    e = cudaStreamEndCapture(b->stream, &b->graph[cls]);
+    if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+    if ((e = cudaGraphInstantiate(&b->exec[cls], b->graph[cls], 0)) != cudaSuccess)
+      return bail(fail(BIRP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  }
   *out = b;
   return ok();
 }
@@ -106,6 +109,7 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n) {
   b->npx.assign(n, 0);
   int64_t used = 0;
   std::vector<double> work(n);
+  int cls = BATCH_CUBE_TRI;
   for (int i = 0; i < n; ++i) {
     const birp_camera& c = reqs[i].cam;
     if (birp_status s = validate_camera(&c)) return s;
@@ -117,6 +121,7 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n) {
     if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, b->d_out + used, rq[i])) return s;
     used += npx;
     work[i] = (double)npx * c.n_samples * (reqs[i].cmem ? 16.0 : 1.0);
+    if (reqs[i].cmem || !c.trilinear) cls = BATCH_ANY;
   }
   // largest work first, so long renders start early and small ones fill the tail
   std::iota(order, order + n, 0);
@@ -129,7 +134,7 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n) {
   b->used = used;
   cudaError_t e;
   if ((e = cudaEventRecord(b->e_start, b->stream)) != cudaSuccess ||
-      (e = cudaGraphLaunch(b->exec, b->stream)) != cudaSuccess ||
+      (e = cudaGraphLaunch(b->exec[cls], b->stream)) != cudaSuccess ||
       (e = cudaEventRecord(b->e_kernel, b->stream)) != cudaSuccess ||
       (used > 0 && (e = cudaMemcpyAsync(b->h_out, b->d_out, (size_t)used * sizeof(float), cudaMemcpyDeviceToHost,
                                         b->stream)) != cudaSuccess) ||

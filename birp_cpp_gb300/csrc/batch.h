@@ -17,11 +17,12 @@ struct birp_batch {
   std::vector<int64_t> npx;
   int n = 0;
   int64_t used = 0;
-  int grid = 0;
+  int grid[2] = {0, 0};
   bool pending = false;
   cudaStream_t stream = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  // one graph per persistent-kernel class (birp::BatchClass)
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};
   cudaEvent_t e_start = nullptr, e_kernel = nullptr, e_end = nullptr;
 };
 

@@ -1,10 +1,11 @@
 // Internal host/device structures of the GB300 render path.
 //
 // Data layout in HBM (one cube):
-//  * values: FP32, x fastest, padded by one guard node on every side
-//    (dims (nx+2) x (ny+2) x (nz+2)); a guard node repeats its edge neighbour,
-//    so a cell index that FP32 rounding puts one step outside [0, n-2] still
-//    reads in-bounds memory and interpolates continuously.
+//  * values: FP32 pairs {v[x], v[x+1]} per node (float2, 8-byte aligned), x
+//    fastest, padded by one guard node on every side (dims (nx+2) x (ny+2) x
+//    (nz+2)); a guard node repeats its edge neighbour, so a cell index that
+//    FP32 rounding puts one step outside [0, n-2] still reads in-bounds memory
+//    and interpolates continuously. A cell's 8 corners are 4 pair loads.
 //  * per-axis index tables (LUT) for nonuniform axes: float4 bins of width at
 //    most the smallest cell, each holding one piecewise-linear index map.
 //  * FP64 axis coordinates, read only by the exact (FP64) decisions.
@@ -33,13 +34,17 @@ struct AxisDev {
 
 struct CubeDev {
   AxisDev ax[3];
-  const float* vals;    // guard-padded grid (see above)
+  const float2* pv;     // guard-padded pair grid (see above)
   uint32_t px;          // nx + 2
   uint32_t pxy;         // (nx + 2) * (ny + 2)
   uint32_t max_off;     // largest valid base offset for an 8-corner fetch
   uint32_t bias;        // folds the FP32 magic-floor bias and the guard shift
   int all_uniform;
   const float4* lut;    // concatenated LUT bins (nullptr if all uniform)
+  // per axis, per cell k in [0, n-2]: {c_k, 1/(c_{k+1}-c_k), c_{k+1}, -c_k/(c_{k+1}-c_k)}
+  // in FP32, for marching cell by cell along a ray; entries -1 and n-1 are
+  // sentinels (x = -inf, resp. z = +inf) that stop the march at the box edge
+  const float4* cells[3];
 };
 
 // CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
@@ -103,9 +108,13 @@ struct BatchDev {
 
 // Host-side launch helpers (render.cu).
 cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaStream_t stream);
-cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream);
-int persistent_grid(int seg_mix_max);
+// Persistent batch kernel classes: CUBE_TRI renders only trilinear cube
+// requests (fewer registers, more resident warps); ANY renders every kind.
+enum BatchClass : int { BATCH_CUBE_TRI = 0, BATCH_ANY = 1 };
+cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
+int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
+cudaError_t launch_cube_pairs(const float* padded, size_t total, float2* pairs, cudaStream_t stream);
 cudaError_t launch_cube_sample(const CubeDev* cube, int trilinear, const float* xyz, int n, float* out,
                                cudaStream_t stream);
 cudaError_t launch_cmem_sample(const CmemDev* cmem, const float* xyz, int n, float* out, cudaStream_t stream);

@@ -48,7 +48,7 @@ birp_status setup_device(int dev, unsigned char** addr, int* grid) {
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
     g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-    g_grid[dev] = persistent_grid(0);
+    g_grid[dev] = persistent_grid(BATCH_ANY);
   }
   *addr = g_scratch_addr[dev];
   *grid = g_grid[dev];

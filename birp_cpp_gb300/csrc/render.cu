@@ -310,14 +310,21 @@ __device__ int exact_cell(const AxisDev& a, double x, int guess) {
 // ---------------------------------------------------------------- one tile
 
 enum Interp { NEAREST = 0, TRILINEAR = 1 };
-enum Axes { AXES_UNIFORM = 0, AXES_LUT = 1 };
+// Axis handling of the cube march: UNIFORM computes the index affinely, LUT
+// through the index tables, DDA walks cell by cell along the ray (any axes;
+// trilinear only).
+enum Axes { AXES_UNIFORM = 0, AXES_LUT = 1, AXES_DDA = 2 };
 
-template <int KIND, int INTERP, int AXES, int SEGL2>
+// One pixel tile of one request. The lanes-per-ray split S = 2^seg_log2 is a
+// runtime value of the request (it only sets the tile shape, the lane -> ray
+// map, the sample stride and the merge); the march itself is S-independent.
+template <int KIND, int INTERP, int AXES>
 __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty, TileSmem& sm,
                                             KernelStats* stats) {
-  constexpr int S = 1 << SEGL2;
-  constexpr int WBX = wb_x(SEGL2), WBY = wb_y(SEGL2);
-  constexpr int TW = 2 * WBX, TH = 2 * WBY;
+  const int SEGL2 = R.seg_log2;
+  const int S = 1 << SEGL2;
+  const int WBX = wb_x(SEGL2), WBY = wb_y(SEGL2);
+  const int TW = 2 * WBX, TH = 2 * WBY;
   const int tid = threadIdx.x;
   const int x0 = tx * TW, y0 = ty * TH;
   const int nx = R.nx, ny = R.ny;
@@ -424,9 +431,98 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   float fi = (float)first;
   const float fS = (float)S;
 
-  if constexpr (KIND == SPACE_CUBE) {
+  if constexpr (KIND == SPACE_CUBE && AXES == AXES_DDA) {
+    // Cell-by-cell march. Along a ray each coordinate is monotone, so per
+    // axis the current cell k, its inverse width, -c_k/width and the next
+    // node in the direction of travel stay in registers; a sample computes
+    // x (one FMA), tests the next node (one FMA + compare) and the cell
+    // fraction (one FMA); crossing a node reads one float4 of the axis' cell
+    // table. The four corner-row pointers advance with the cells, so the 8
+    // gathers need no address arithmetic. k stays in [0, n-2], so every
+    // gather is in bounds by construction.
     const CubeDev& C = *R.cube;
-    const float* __restrict__ vals = C.vals;
+    float st[3], bs[3], sg[3], iw[3], ncl[3], ncs[3];
+    const float4* cell[3];
+    int dstr[3];
+    const float2* p00 = C.pv;
+    if (iters > 0) {
+      long long off = (long long)C.pxy + C.px + 1;
+      const int stride[3] = {1, (int)C.px, (int)C.pxy};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const AxisDev& A = C.ax[k];
+        st[k] = R.dt32 * d32[k] * fS;
+        bs[k] = fmaf(fi, R.dt32 * d32[k], fmaf(0.5f, R.dt32 * d32[k], R.pos32[k]));
+        sg[k] = d32[k] >= 0.f ? 1.f : -1.f;
+        const float x0 = bs[k];
+        float idx = A.uniform ? (x0 - A.c0) * A.inv_h : lut_index(A, C.lut, x0);
+        int kb;
+        magic_floor(fminf(fmaxf(idx, 0.f), (float)(A.n - 2)), kb);
+        const int k0 = kb - kMagicBits;
+        cell[k] = C.cells[k] + k0;
+        const float4 e = __ldg(cell[k]);
+        iw[k] = e.y;
+        ncl[k] = e.w;
+        ncs[k] = sg[k] > 0.f ? -e.z : e.x;
+        dstr[k] = sg[k] > 0.f ? stride[k] : -stride[k];
+        off += (long long)k0 * stride[k];
+      }
+      p00 = C.pv + off;
+    }
+    const float2* p01 = p00 + C.px;
+    const float2* p10 = p00 + C.pxy;
+    const float2* p11 = p10 + C.px;
+    // One sample at iteration fit: advance the cells (one branch for all
+    // three axes: the largest crossing test decides), then fetch and
+    // interpolate.
+    auto sample = [&](float fit) -> float {
+      float x[3], cr[3], fr[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        x[k] = fmaf(fit, st[k], bs[k]);
+        cr[k] = fmaf(x[k], sg[k], ncs[k]);
+      }
+      if (fmaxf(fmaxf(cr[0], cr[1]), cr[2]) >= 0.f) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          // crossed the next node: step cells until x is inside (the
+          // sentinels end the walk at the box edge)
+          while (fmaf(x[k], sg[k], ncs[k]) >= 0.f) {
+            cell[k] += (sg[k] > 0.f ? 1 : -1);
+            const float4 e = __ldg(cell[k]);
+            iw[k] = e.y;
+            ncl[k] = e.w;
+            ncs[k] = sg[k] > 0.f ? -e.z : e.x;
+            p00 += dstr[k];
+            p01 += dstr[k];
+            p10 += dstr[k];
+            p11 += dstr[k];
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) fr[k] = fmaf(x[k], iw[k], ncl[k]);
+      const float2 c00 = __ldg(p00), c01 = __ldg(p01), c10 = __ldg(p10), c11 = __ldg(p11);
+      const float lx1 = lerp_f(c00.x, c00.y, fr[0]), lx2 = lerp_f(c01.x, c01.y, fr[0]);
+      const float hx1 = lerp_f(c10.x, c10.y, fr[0]), hx2 = lerp_f(c11.x, c11.y, fr[0]);
+      const float ly1 = lerp_f(lx1, lx2, fr[1]), hy1 = lerp_f(hx1, hx2, fr[1]);
+      return lerp_f(ly1, hy1, fr[2]);
+    };
+    // samples in pairs: the pair sum enters the compensated sum, halving the
+    // serial Kahan chain
+    float fit = 0.f;  // iteration count as float (no conversion per sample)
+    int it = 0;
+    for (; it + 1 < iters; it += 2) {
+      const float va = sample(fit);
+      const float vb = sample(fit + 1.f);
+      acc.add(va + vb);
+      fit += 2.f;
+    }
+    if (it < iters) acc.add(sample(fit));
+  } else if constexpr (KIND == SPACE_CUBE) {
+    // nearest by truncation (UNIFORM / LUT index)
+    const CubeDev& C = *R.cube;
+    const float* __restrict__ vals = reinterpret_cast<const float*>(C.pv);  // .x of pair i at 2i
     const uint32_t px = C.px, pxy = C.pxy, bias = C.bias, max_off = C.max_off;
     float st[3], bs[3];
 #pragma unroll
@@ -471,19 +567,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       float flz = magic_floor(idx[2], bz);
       float fx = idx[0] - flx, fy = idx[1] - fly, fz = idx[2] - flz;
       float v;
-      if constexpr (INTERP == TRILINEAR) {
-        uint32_t off = (uint32_t)bz * pxy + (uint32_t)by * px + (uint32_t)bx + bias;
-        off = min(off, max_off);
-        const float* p = vals + off;
-        float c000 = __ldg(p), c001 = __ldg(p + 1);
-        float c010 = __ldg(p + px), c011 = __ldg(p + px + 1);
-        float c100 = __ldg(p + pxy), c101 = __ldg(p + pxy + 1);
-        float c110 = __ldg(p + pxy + px), c111 = __ldg(p + pxy + px + 1);
-        float lx1 = lerp_f(c000, c001, fx), lx2 = lerp_f(c010, c011, fx);
-        float hx1 = lerp_f(c100, c101, fx), hx2 = lerp_f(c110, c111, fx);
-        float ly1 = lerp_f(lx1, lx2, fy), hy1 = lerp_f(hx1, hx2, fy);
-        v = lerp_f(ly1, hy1, fz);
-      } else {
+      static_assert(INTERP == NEAREST, "trilinear cubes march with AXES_DDA");
+      {
         float eps_cell = fmaf(fi, eps_slope, eps_base);
         bool unsure = !(fminf(fminf(fx, 1.f - fx), fminf(fminf(fy, 1.f - fy), fminf(fz, 1.f - fz))) >= eps_cell);
         if (unsure) {
@@ -500,7 +585,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         }
         uint32_t off = (uint32_t)bz * pxy + (uint32_t)by * px + (uint32_t)bx + bias;
         off = min(off, max_off);
-        v = __ldg(vals + off);
+        v = __ldg(vals + 2 * (size_t)off);
       }
       acc.add(v);
       fi += fS;
@@ -540,8 +625,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   }
   // merge the S partial sums of a ray
   float hi = acc.s, lo = -acc.c;
-#pragma unroll
-  for (int o = S >> 1; o >= 1; o >>= 1) {
+  for (int o = S >> 1; o >= 1; o >>= 1) {  // S is uniform across the warp
     float oh = __shfl_xor_sync(0xffffffffu, hi, o);
     float ol = __shfl_xor_sync(0xffffffffu, lo, o);
     float s, e;
@@ -554,48 +638,32 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 }
 
 // One request, one CTA per tile; the request travels as a kernel parameter.
-template <int KIND, int INTERP, int AXES, int SEGL2>
+template <int KIND, int INTERP, int AXES>
 __global__ void __launch_bounds__(kThreads) render_plain_kernel(const RequestDev req, KernelStats* stats) {
   __shared__ TileSmem sm;
-  render_tile<KIND, INTERP, AXES, SEGL2>(req, blockIdx.x, blockIdx.y, sm, stats);
+  render_tile<KIND, INTERP, AXES>(req, blockIdx.x, blockIdx.y, sm, stats);
 }
 
 // Dispatch over the request's variant.
-template <int SEGL2>
-__device__ __forceinline__ void render_tile_any_cube(const RequestDev& R, int tx, int ty, TileSmem& sm,
-                                                     KernelStats* st) {
-  const bool lut = R.axes_lut != 0;
-  if (R.interp) {
-    if (lut) render_tile<SPACE_CUBE, TRILINEAR, AXES_LUT, SEGL2>(R, tx, ty, sm, st);
-    else render_tile<SPACE_CUBE, TRILINEAR, AXES_UNIFORM, SEGL2>(R, tx, ty, sm, st);
-  } else {
-    if (lut) render_tile<SPACE_CUBE, NEAREST, AXES_LUT, SEGL2>(R, tx, ty, sm, st);
-    else render_tile<SPACE_CUBE, NEAREST, AXES_UNIFORM, SEGL2>(R, tx, ty, sm, st);
-  }
-}
-
 __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& sm, KernelStats* st) {
   if (R.kind == SPACE_CMEM) {
-    switch (R.seg_log2) {
-      case 0: render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 0>(R, tx, ty, sm, st); break;
-      case 1: render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 1>(R, tx, ty, sm, st); break;
-      case 2: render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 2>(R, tx, ty, sm, st); break;
-      default: render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 3>(R, tx, ty, sm, st); break;
-    }
-    return;
-  }
-  switch (R.seg_log2) {
-    case 0: render_tile_any_cube<0>(R, tx, ty, sm, st); break;
-    case 1: render_tile_any_cube<1>(R, tx, ty, sm, st); break;
-    case 2: render_tile_any_cube<2>(R, tx, ty, sm, st); break;
-    default: render_tile_any_cube<3>(R, tx, ty, sm, st); break;
+    render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM>(R, tx, ty, sm, st);
+  } else if (R.interp) {
+    render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, st);
+  } else if (R.axes_lut) {
+    render_tile<SPACE_CUBE, NEAREST, AXES_LUT>(R, tx, ty, sm, st);
+  } else {
+    render_tile<SPACE_CUBE, NEAREST, AXES_UNIFORM>(R, tx, ty, sm, st);
   }
 }
 
 // Persistent batch kernel: CTAs pull (request, tile) items from a device
 // queue head until the batch is exhausted. No waits: each CTA exits when the
-// queue is empty. Items are numbered in the host's order (largest work first).
-__global__ void __launch_bounds__(kThreads) render_batch_kernel(BatchDev B) {
+// queue is empty. Items are numbered in the host's order (largest work
+// first). CLS = BATCH_CUBE_TRI compiles only the trilinear cube march (fewer
+// registers, more resident warps); BATCH_ANY renders every request kind.
+template <int CLS>
+__global__ void __launch_bounds__(kThreads, CLS == BATCH_CUBE_TRI ? 8 : 1) render_batch_kernel(BatchDev B) {
   __shared__ TileSmem sm;
   __shared__ int s_item;
   const int n_reqs = __ldg(B.hdr), total_items = __ldg(B.hdr + 1);
@@ -616,7 +684,11 @@ __global__ void __launch_bounds__(kThreads) render_batch_kernel(BatchDev B) {
     const RequestDev& R = B.reqs[__ldg(B.order + lo)];
     const int t = item - __ldg(B.first + lo);
     const int tx = t % R.tiles_x, ty = t / R.tiles_x;
-    render_tile_any(R, tx, ty, sm, B.stats);
+    if constexpr (CLS == BATCH_CUBE_TRI) {
+      render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, B.stats);
+    } else {
+      render_tile_any(R, tx, ty, sm, B.stats);
+    }
   }
 }
 
@@ -654,6 +726,13 @@ __global__ void cube_guard_kernel(float* dst, int nx, int ny, int nz) {
   }
 }
 
+// Pair grid from the padded scalar grid: pair i = {v[i], v[i+1]} (the last
+// node of each row is never the left corner of a cell).
+__global__ void cube_pairs_kernel(const float* __restrict__ v, size_t total, float2* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = make_float2(v[i], v[i + 1 < total ? i + 1 : i]);
+}
+
 // DataCube::GetSample for a batch of points: exact FP64 in-box test and cell
 // choice, FP64 interpolation, -1 outside the box.
 __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int trilinear, const float* __restrict__ xyz,
@@ -683,14 +762,14 @@ __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int triline
       out[t] = -1.f;
       continue;
     }
-    const float* b = C.vals + ((size_t)(k[2] + 1) * C.pxy + (size_t)(k[1] + 1) * C.px + (k[0] + 1));
+    const float2* b = C.pv + ((size_t)(k[2] + 1) * C.pxy + (size_t)(k[1] + 1) * C.px + (k[0] + 1));
     if (!trilinear) {
-      out[t] = b[0];
+      out[t] = b[0].x;
       continue;
     }
     auto L = [](double u, double v, double w) { return u + w * (v - u); };
-    double lx1 = L(b[0], b[1], f[0]), lx2 = L(b[C.px], b[C.px + 1], f[0]);
-    double hx1 = L(b[C.pxy], b[C.pxy + 1], f[0]), hx2 = L(b[C.pxy + C.px], b[C.pxy + C.px + 1], f[0]);
+    double lx1 = L(b[0].x, b[0].y, f[0]), lx2 = L(b[C.px].x, b[C.px].y, f[0]);
+    double hx1 = L(b[C.pxy].x, b[C.pxy].y, f[0]), hx2 = L(b[C.pxy + C.px].x, b[C.pxy + C.px].y, f[0]);
     out[t] = (float)L(L(lx1, lx2, f[1]), L(hx1, hx2, f[1]), f[2]);
   }
 }
@@ -784,47 +863,29 @@ int tile_w(int segl2) { return tw_of(segl2); }
 int tile_h(int segl2) { return th_of(segl2); }
 
 cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStream_t s) {
-  const RequestDev& d = h;
   dim3 grid((h.nx + tw_of(h.seg_log2) - 1) / tw_of(h.seg_log2), (h.ny + th_of(h.seg_log2) - 1) / th_of(h.seg_log2));
-  if (h.kind == SPACE_CMEM) {
-    switch (h.seg_log2) {
-      case 0: render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 0><<<grid, kThreads, 0, s>>>(d, stats); break;
-      case 1: render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 1><<<grid, kThreads, 0, s>>>(d, stats); break;
-      case 2: render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 2><<<grid, kThreads, 0, s>>>(d, stats); break;
-      default: render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_UNIFORM, 3><<<grid, kThreads, 0, s>>>(d, stats); break;
-    }
-    return cudaGetLastError();
-  }
-  const bool lut = h.axes_lut != 0;
-#define BIRP_LAUNCH_CUBE(SEG)                                                                                   \
-  if (h.interp) {                                                                                               \
-    if (lut) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_LUT, SEG><<<grid, kThreads, 0, s>>>(d, stats);     \
-    else render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_UNIFORM, SEG><<<grid, kThreads, 0, s>>>(d, stats);     \
-  } else {                                                                                                      \
-    if (lut) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_LUT, SEG><<<grid, kThreads, 0, s>>>(d, stats);       \
-    else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_UNIFORM, SEG><<<grid, kThreads, 0, s>>>(d, stats);       \
-  }
-  switch (h.seg_log2) {
-    case 0: BIRP_LAUNCH_CUBE(0) break;
-    case 1: BIRP_LAUNCH_CUBE(1) break;
-    case 2: BIRP_LAUNCH_CUBE(2) break;
-    default: BIRP_LAUNCH_CUBE(3) break;
-  }
-#undef BIRP_LAUNCH_CUBE
+  if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_UNIFORM><<<grid, kThreads, 0, s>>>(h, stats);
+  else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, stats);
+  else if (h.axes_lut) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_LUT><<<grid, kThreads, 0, s>>>(h, stats);
+  else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_UNIFORM><<<grid, kThreads, 0, s>>>(h, stats);
   return cudaGetLastError();
 }
 
-int persistent_grid(int) {
+int persistent_grid(int cls) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel, kThreads, 0);
+  if (cls == BATCH_CUBE_TRI)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI>, kThreads, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_ANY>, kThreads, 0);
   if (per_sm < 1) per_sm = 1;
   return sms * per_sm;
 }
 
-cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s) {
-  render_batch_kernel<<<grid, kThreads, 0, s>>>(b);
+cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int cls) {
+  if (cls == BATCH_CUBE_TRI) render_batch_kernel<BATCH_CUBE_TRI><<<grid, kThreads, 0, s>>>(b);
+  else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b);
   return cudaGetLastError();
 }
 
@@ -832,6 +893,12 @@ cudaError_t launch_cube_fill(const float*, int nx, int ny, int nz, float* dst, c
   long long total = 2ll * (nx + 2) * (ny + 2) + 2ll * (nx + 2) * nz + 2ll * ny * nz;
   int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
   cube_guard_kernel<<<blocks, 256, 0, s>>>(dst, nx, ny, nz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cube_pairs(const float* padded, size_t total, float2* pairs, cudaStream_t s) {
+  int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
+  cube_pairs_kernel<<<blocks, 256, 0, s>>>(padded, total, pairs);
   return cudaGetLastError();
 }
 

@@ -140,3 +140,34 @@ def config2_requests(n: int = 512, seed: int = 2):
     steps = rng.integers(0, len(STEPS), n)
     return [(tuple(pos[i]), (9.0, 0.0, 0.0), SIZES[sizes[i]][0], SIZES[sizes[i]][1], STEPS[steps[i]])
             for i in range(n)]
+
+
+def cube_stretched(nx: int, ny: int, nz: int, r0: float, seed: int, noise: float = 0.3):
+    """A cube with the config-1 axis rule on x in [-40, 30], y, z in [-40, 40]
+    and its own magnetopause standoff r0 (bow shock at 1.3 r0)."""
+    rng = np.random.default_rng(seed)
+    xs, ys, zs = stretched_axis(-40, 30, nx), stretched_axis(-40, 40, ny), stretched_axis(-40, 40, nz)
+    return xs, ys, zs, sheath_field(xs, ys, zs, rng, r0=r0, noise=noise)
+
+
+def config3_specs(n_cubes: int = 48, cams_per_cube: int = 16, n_cmem: int = 8, seed: int = 3):
+    """Uneven multi-cube batch: per cube (nx, ny, nz) drawn from multiples of 16
+    in [96, 320], standoff r0 in U[7, 12]; each cube gets `cams_per_cube`
+    requests from config 2's orbit/size/step sampler; `n_cmem` gridless CMEM
+    requests from the same sampler. Returns (cubes, requests) where cubes are
+    (nx, ny, nz, r0, seed) and requests are (source, pos, aim, nx, ny, step)
+    with source an index into cubes or -1 for CMEM."""
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(96 // 16, 320 // 16 + 1, size=(n_cubes, 3)) * 16
+    r0s = rng.uniform(7.0, 12.0, n_cubes)
+    cubes = [(int(d[0]), int(d[1]), int(d[2]), float(r), int(1000 + i)) for i, (d, r) in enumerate(zip(dims, r0s))]
+    reqs = []
+    cams = config2_requests(n_cubes * cams_per_cube + n_cmem, seed=seed + 1)
+    for i in range(n_cubes):
+        for j in range(cams_per_cube):
+            pos, aim, nx, ny, step = cams[i * cams_per_cube + j]
+            reqs.append((i, pos, aim, nx, ny, step))
+    for j in range(n_cmem):
+        pos, aim, nx, ny, step = cams[n_cubes * cams_per_cube + j]
+        reqs.append((-1, pos, aim, nx, ny, step))
+    return cubes, reqs
