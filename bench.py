@@ -136,6 +136,133 @@ def make_workload(B, n_req: int, seed_cube: int = 1, seed_req: int = 2):
     return dict(cube=cube, cams=cams, reqs=reqs, host=(xs, ys, zs, v32))
 
 
+def _gen_cube(spec):
+    from birp_cpp_gb300 import synth
+    nx, ny, nz, r0, seed = spec
+    xs, ys, zs, v = synth.cube_stretched(nx, ny, nz, r0, seed)
+    return xs, ys, zs, v.astype(np.float32)
+
+
+def make_workload_c3(B, host_cubes, specs):
+    """Config 3: 48 uneven stretched cubes (16 cameras each) + 8 CMEM requests."""
+    from birp_cpp_gb300 import synth
+    cubes = [B.Cube(*hc) for hc in host_cubes]
+    cmem = B.Cmem()
+    items = []
+    for src, pos, aim, nx, ny, step in specs:
+        cam = B.camera(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(step),
+                       ray_length=synth.RAY_LENGTH, trilinear=True)
+        items.append((cubes[src] if src >= 0 else cmem, cam))
+    return cubes, cmem, items
+
+
+def run_c3(args, B):
+    """One-launch multi-cube batch (config 3) vs plain renders of the same requests."""
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    from birp_cpp_gb300 import synth
+    cube_specs, specs = synth.config3_specs()
+    with cf.ProcessPoolExecutor(max_workers=os.cpu_count() or 4, mp_context=mp.get_context("spawn")) as ex:
+        host = list(ex.map(_gen_cube, cube_specs))
+    from birp_cpp_gb300 import build
+    build.build()
+    B.init(0)
+    cubes, cmem, items = make_workload_c3(B, host, specs)
+    total_px = sum(c.nx * c.ny for _, c in items)
+    batch = B.Batch(len(items), total_px)
+    for _ in range(max(args.warmup, 2)):
+        batch.render(items)
+    km = []
+    for _ in range(args.steps):
+        B.flush_l2()
+        batch.submit(items)
+        batch.wait()
+        km.append(batch.last_ms()[0])
+    ms = float(np.mean(km))
+    outs = [np.empty((c.ny, c.nx), np.float32) for _, c in items]
+    t0 = time.perf_counter()
+    for (sp, c), o in zip(items, outs):
+        B.render(sp, c, out=o)
+    plain_s = time.perf_counter() - t0
+    dev_bytes = sum(c.info().device_bytes for c in cubes)
+    print(json.dumps({"workload": "config 3: 48 uneven stretched cubes x 16 cameras + 8 CMEM, one launch",
+                      "requests": len(items), "images_s": len(items) / (ms / 1000), "ms_per_launch": ms,
+                      "plain_images_s": len(items) / plain_s, "batched_vs_plain": (len(items) / (ms / 1000)) /
+                      (len(items) / plain_s), "cube_device_bytes": dev_bytes}))
+
+
+def run_c4(args, B):
+    """Serving sweep (config 4): Poisson arrivals at each rate for a fixed time;
+    requests pick a cube by Zipf(1.1) popularity over a pool of cubes held in
+    host (pinned) memory, rendered through the server under a GPU byte budget
+    with LRU eviction; poses, sizes and steps from the orbit sampler.
+    Reports images/s and p50/p99 latency per rate beside the plain per-call
+    render's latency."""
+    from birp_cpp_gb300 import build, synth
+    nx, ny, nz = (int(v) for v in args.c4_dims.split("x"))
+    rng = np.random.default_rng(4)
+    # a few base fields (standoff r0 groups) and per-cube sheath noise
+    xs, ys, zs = synth.stretched_axis(-40, 30, nx), synth.stretched_axis(-40, 40, ny), synth.stretched_axis(-40, 40, nz)
+    r0_groups = [7.5, 9.0, 10.5, 12.0]
+    bases = [synth.sheath_field(xs, ys, zs, np.random.default_rng(40 + g), r0=r0, noise=0.0).astype(np.float32)
+             for g, r0 in enumerate(r0_groups)]
+    build.build()
+    B.init(0)
+    srv = B.Server(B.server_config(cube_budget_bytes=int(args.c4_budget_gb * (1 << 30)), slots=3,
+                                   max_batch_requests=64, max_batch_pixels=16 << 20, max_wait_ms=1.0,
+                                   max_queue=1 << 16))
+    ids = []
+    for i in range(args.c4_cubes):
+        base = bases[i % len(bases)]
+        noise = (1.0 + 0.3 * rng.uniform(-1, 1, base.shape).astype(np.float32))
+        ids.append(srv.add_cube(xs, ys, zs, base * noise))
+        del noise
+    zipf_w = 1.0 / np.arange(1, args.c4_cubes + 1) ** 1.1
+    zipf_w /= zipf_w.sum()
+    reqs = synth.config2_requests(8192, seed=44)
+    cams = [B.camera(p, a, synth.FOV_W, synth.FOV_H, w, h, n_samples=synth.n_samples(st)) for p, a, w, h, st in reqs]
+    max_px = max(c.nx * c.ny for c in cams)
+    bufs = [np.empty(max_px, np.float32) for _ in range(1024)]
+    results = []
+    for rate in (float(r) for r in args.c4_rates.split(",")):
+        t0 = time.perf_counter()
+        nxt, k, tickets = t0, 0, []
+        st0 = srv.stats()
+        while nxt - t0 < args.c4_seconds:
+            now = time.perf_counter()
+            if now < nxt:
+                time.sleep(min(nxt - now, 0.002))
+                continue
+            cid = ids[int(rng.choice(args.c4_cubes, p=zipf_w))]
+            try:
+                tickets.append(srv.submit(cid, cams[k % len(cams)], bufs[k % len(bufs)]))
+            except B.BirpError:
+                pass
+            k += 1
+            nxt += rng.exponential(1.0 / rate)
+        lat = [r.latency_ms for r in (srv.wait(t, 120000) for t in tickets) if r.status == 0]
+        t1 = time.perf_counter()
+        st1 = srv.stats()
+        lat = np.array(lat) if lat else np.zeros(1)
+        results.append({"offered_req_s": rate, "completed": len(lat), "images_s": len(lat) / (t1 - t0),
+                        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                        "uploads": st1.cube_uploads - st0.cube_uploads, "evictions": st1.cube_evictions - st0.cube_evictions,
+                        "hits": st1.cube_hits - st0.cube_hits, "rejected": st1.rejected - st0.rejected})
+        print(json.dumps(results[-1]), flush=True)
+    srv.close()
+    # plain per-call latency on one resident cube
+    cube = B.Cube(xs, ys, zs, bases[0])
+    pl = []
+    for c in cams[:200]:
+        t = time.perf_counter()
+        B.render(cube, c, out=bufs[0][: c.nx * c.ny].reshape(c.ny, c.nx))
+        pl.append(1000 * (time.perf_counter() - t))
+    print(json.dumps({"workload": f"config 4 serving sweep: {args.c4_cubes} cubes of {nx}x{ny}x{nz}, Zipf(1.1), "
+                                  f"{args.c4_budget_gb} GB budget, {args.c4_seconds} s per rate",
+                      "sweep": results, "plain_p50_ms": float(np.percentile(pl, 50)),
+                      "plain_p99_ms": float(np.percentile(pl, 99)), "plain_images_s": len(pl) / (sum(pl) / 1000)}))
+
+
 def cpu_sample(reqs, host, seconds: float, threads: int, seed: int = 7):
     """The reference's FP32 render arithmetic (oracle port, per-cell lookup on
     the stretched axes) over random pixels drawn uniformly from all pixels of
@@ -224,10 +351,22 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--serve-seconds", type=float, default=3.0)
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
+                    help="c2: the 512-request single-cube batch (default); c3: 48-cube + CMEM batch; "
+                         "c4: serving sweep")
+    ap.add_argument("--c4-cubes", type=int, default=64)
+    ap.add_argument("--c4-dims", default="512x384x384")
+    ap.add_argument("--c4-budget-gb", type=float, default=60.0)
+    ap.add_argument("--c4-rates", default="50,200,500,1000,2000")
+    ap.add_argument("--c4-seconds", type=float, default=10.0)
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, world, rank)
+        return
+    if args.workload in ("c3", "c4"):
+        import birp_cpp_gb300 as B
+        (run_c3 if args.workload == "c3" else run_c4)(args, B)
         return
 
     import birp_cpp_gb300 as B

@@ -18,10 +18,10 @@ struct birp_cube {
   double min_gap[3] = {0, 0, 0};
   birp::CubeDev h_desc{};       // host copy of the device descriptor
   birp::CubeDev* d_desc = nullptr;
-  float2* d_vals = nullptr;     // pair grid (birp_internal.h)
+  float4* d_vals = nullptr;     // cell records (birp_internal.h)
   double* d_c64 = nullptr;      // 3 axes, concatenated
   float4* d_lut = nullptr;
-  float4* d_cells = nullptr;    // per-cell march tables, 3 axes concatenated
+  float2* d_cells = nullptr;    // per-cell march tables, 3 axes concatenated
   size_t device_bytes = 0;
   cudaStream_t alloc_stream = nullptr;  // non-null: stream-ordered (pool) allocations
 };

@@ -1,11 +1,16 @@
 // Internal host/device structures of the GB300 render path.
 //
 // Data layout in HBM (one cube):
-//  * values: FP32 pairs {v[x], v[x+1]} per node (float2, 8-byte aligned), x
-//    fastest, padded by one guard node on every side (dims (nx+2) x (ny+2) x
-//    (nz+2)); a guard node repeats its edge neighbour, so a cell index that
-//    FP32 rounding puts one step outside [0, n-2] still reads in-bounds memory
-//    and interpolates continuously. A cell's 8 corners are 4 pair loads.
+//  * values: one 32-byte record per cell holding the 8 coefficients of its
+//    trilinear polynomial f(x,y,z) = c0 + c1 x + c2 y + c3 z + c4 xy + c5 xz
+//    + c6 yz + c7 xyz (x, y, z the cell fractions), computed in FP64 from the
+//    FP32 corner values and stored FP32 as {c0, c1, c2, c4 | c3, c5, c6, c7};
+//    c0 is the value of the cell's lower corner (node k). Records are x
+//    fastest for cells -1..n-1 on every axis (one guard cell each side whose
+//    outside corners repeat the edge node), so a cell index that FP32
+//    rounding puts one step outside [0, n-2] still reads in-bounds memory and
+//    interpolates continuously. A sample is two 16-byte loads from one
+//    pointer and 7 FMAs.
 //  * per-axis index tables (LUT) for nonuniform axes: float4 bins of width at
 //    most the smallest cell, each holding one piecewise-linear index map.
 //  * FP64 axis coordinates, read only by the exact (FP64) decisions.
@@ -34,17 +39,16 @@ struct AxisDev {
 
 struct CubeDev {
   AxisDev ax[3];
-  const float2* pv;     // guard-padded pair grid (see above)
-  uint32_t px;          // nx + 2
-  uint32_t pxy;         // (nx + 2) * (ny + 2)
-  uint32_t max_off;     // largest valid base offset for an 8-corner fetch
-  uint32_t bias;        // folds the FP32 magic-floor bias and the guard shift
+  const float4* rec;    // cell records, 2 float4 each (see above)
+  uint32_t cx;          // records along x: nx + 1
+  uint32_t cxy;         // records per z slab: (nx + 1) * (ny + 1)
   int all_uniform;
   const float4* lut;    // concatenated LUT bins (nullptr if all uniform)
-  // per axis, per cell k in [0, n-2]: {c_k, 1/(c_{k+1}-c_k), c_{k+1}, -c_k/(c_{k+1}-c_k)}
-  // in FP32, for marching cell by cell along a ray; entries -1 and n-1 are
-  // sentinels (x = -inf, resp. z = +inf) that stop the march at the box edge
-  const float4* cells[3];
+  // per axis, per cell k in [0, n-2]: {1/(c_{k+1}-c_k), -c_k/(c_{k+1}-c_k)} in
+  // FP32 (the cell fraction is x * first + second), for marching cell by cell
+  // along a ray; entries -1 and n-1 are sentinels {0, 1} and {0, 0} whose
+  // fraction never leaves [0, 1], which stops the march at the box edge
+  const float2* cells[3];
 };
 
 // CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
@@ -114,7 +118,7 @@ enum BatchClass : int { BATCH_CUBE_TRI = 0, BATCH_ANY = 1 };
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
-cudaError_t launch_cube_pairs(const float* padded, size_t total, float2* pairs, cudaStream_t stream);
+cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, float4* rec, cudaStream_t stream);
 cudaError_t launch_cube_sample(const CubeDev* cube, int trilinear, const float* xyz, int n, float* out,
                                cudaStream_t stream);
 cudaError_t launch_cmem_sample(const CmemDev* cmem, const float* xyz, int n, float* out, cudaStream_t stream);

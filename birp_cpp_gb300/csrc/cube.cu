@@ -137,32 +137,32 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
 
   size_t coords = (size_t)nx + ny + nz;
   // per-cell march table of every axis: cells 0..n-2 between two sentinels
-  // whose crossing test never fires (a cell pointer cannot leave [-1, n-1],
-  // whose corners all lie in the guard-padded grid)
-  std::vector<float4> cells;
+  // (iw = 0, fraction fixed at 1 below and 0 above: the walk stops there; a
+  // cell pointer cannot leave [-1, n-1], whose records all exist)
+  std::vector<float2> cells;
   cells.reserve(coords + 3);
   size_t cell_off[3];
   for (int k = 0; k < 3; ++k) {
     const std::vector<double>& ck = c.c[k];
     const int n = c.n[k];
-    const double w0 = ck[1] - ck[0], wl = ck[n - 1] - ck[n - 2];
-    cells.push_back(make_float4(-INFINITY, (float)(1.0 / w0), (float)ck[0], (float)(-(ck[0] - w0) / w0)));
+    cells.push_back(make_float2(0.f, 1.f));
     cell_off[k] = cells.size();
     for (int i = 0; i + 1 < n; ++i) {
-      double w = ck[i + 1] - ck[i];
-      double iw = 1.0 / w;
-      cells.push_back(make_float4((float)ck[i], (float)iw, (float)ck[i + 1], (float)(-ck[i] * iw)));
+      double iw = 1.0 / (ck[i + 1] - ck[i]);
+      cells.push_back(make_float2((float)iw, (float)(-ck[i] * iw)));
     }
-    cells.push_back(make_float4((float)ck[n - 1], (float)(1.0 / wl), INFINITY, (float)(-ck[n - 1] / wl)));
+    cells.push_back(make_float2(0.f, 0.f));
   }
-  CKU(dev_alloc(&c.d_cells, cells.size() * sizeof(float4), c.alloc_stream));
-  CKU(dev_alloc(&c.d_vals, total * sizeof(float2), c.alloc_stream));
-  float* scalar = nullptr;  // the padded scalar grid, turned into pairs then freed
+  CKU(dev_alloc(&c.d_cells, cells.size() * sizeof(float2), c.alloc_stream));
+  const size_t records = ((size_t)nx + 1) * ((size_t)ny + 1) * ((size_t)nz + 1);
+  CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
+  float* scalar = nullptr;  // the padded scalar grid, turned into cell records then freed
   CKU(dev_alloc(&scalar, total * sizeof(float), c.alloc_stream));
   CKU(dev_alloc(&c.d_c64, coords * sizeof(double), c.alloc_stream));
   if (!lut.empty()) CKU(dev_alloc(&c.d_lut, lut.size() * sizeof(float4), c.alloc_stream));
   CKU(dev_alloc(&c.d_desc, sizeof(CubeDev), c.alloc_stream));
-  c.device_bytes = total * sizeof(float2) + coords * sizeof(double) + (lut.size() + cells.size()) * sizeof(float4) +
+  c.device_bytes = records * 2 * sizeof(float4) + coords * sizeof(double) + lut.size() * sizeof(float4) +
+                   cells.size() * sizeof(float2) +
                    sizeof(CubeDev);
 
   // interior values: one strided 3D copy from the caller's x-fastest array
@@ -175,7 +175,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   p.kind = cudaMemcpyHostToDevice;
   CKU(cudaMemcpy3DAsync(&p, st));
   CKU(launch_cube_fill(nullptr, nx, ny, nz, scalar, st));
-  CKU(launch_cube_pairs(scalar, total, c.d_vals, st));
+  CKU(launch_cube_records(scalar, nx, ny, nz, c.d_vals, st));
   if (c.alloc_stream) CKU(cudaFreeAsync(scalar, st));
 
   // (the host vectors below stay alive until the synchronize at the end)
@@ -184,7 +184,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   for (int k = 0; k < 3; ++k) all.insert(all.end(), c.c[k].begin(), c.c[k].end());
   CKU(cudaMemcpyAsync(c.d_c64, all.data(), coords * sizeof(double), cudaMemcpyHostToDevice, st));
   if (!lut.empty()) CKU(cudaMemcpyAsync(c.d_lut, lut.data(), lut.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CKU(cudaMemcpyAsync(c.d_cells, cells.data(), cells.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+  CKU(cudaMemcpyAsync(c.d_cells, cells.data(), cells.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
 
   size_t off = 0;
   for (int k = 0; k < 3; ++k) {
@@ -203,12 +203,9 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     a.c64 = c.d_c64 + off;
     off += a.n;
   }
-  d.pv = c.d_vals;
-  d.px = (uint32_t)px;
-  d.pxy = (uint32_t)(px * py);
-  const uint32_t corner = d.pxy + d.px + 1;  // offset of node (0,0,0) in the padded grid
-  d.bias = (uint32_t)((1u - (uint32_t)0x4B400000) * corner);
-  d.max_off = (uint32_t)(total - 1 - corner);
+  d.rec = c.d_vals;
+  d.cx = (uint32_t)(nx + 1);
+  d.cxy = (uint32_t)((nx + 1) * (ny + 1));
   d.lut = c.d_lut;
   for (int k = 0; k < 3; ++k) d.cells[k] = c.d_cells + cell_off[k];
   CKU(cudaMemcpyAsync(c.d_desc, &d, sizeof d, cudaMemcpyHostToDevice, st));
@@ -228,7 +225,8 @@ size_t cube_device_bytes(const birp_cube& c) {
   if (!all_uniform)
     for (int k = 0; k < 3; ++k)
       lut += (size_t)std::max(1.0, std::ceil((c.c[k].back() - c.c[k].front()) / c.min_gap[k])) * sizeof(float4);
-  const size_t cells = (coords + 3) * sizeof(float4);
-  return total * sizeof(float2) + coords * sizeof(double) + lut + cells + sizeof(CubeDev);
+  const size_t cells = (coords + 3) * sizeof(float2);
+  const size_t records = ((size_t)c.n[0] + 1) * ((size_t)c.n[1] + 1) * ((size_t)c.n[2] + 1);
+  return records * 2 * sizeof(float4) + coords * sizeof(double) + lut + cells + sizeof(CubeDev);
 }
 }  // namespace birp

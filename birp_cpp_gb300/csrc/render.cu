@@ -25,6 +25,7 @@
 #include <cstdint>
 
 #include "birp_internal.h"
+#include "cell_index.h"
 
 namespace birp {
 namespace {
@@ -432,81 +433,69 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   const float fS = (float)S;
 
   if constexpr (KIND == SPACE_CUBE && AXES == AXES_DDA) {
-    // Cell-by-cell march. Along a ray each coordinate is monotone, so per
-    // axis the current cell k, its inverse width, -c_k/width and the next
-    // node in the direction of travel stay in registers; a sample computes
-    // x (one FMA), tests the next node (one FMA + compare) and the cell
-    // fraction (one FMA); crossing a node reads one float4 of the axis' cell
-    // table. The four corner-row pointers advance with the cells, so the 8
-    // gathers need no address arithmetic. k stays in [0, n-2], so every
-    // gather is in bounds by construction.
+    // Cell-by-cell march in fraction space. Along a ray each coordinate is
+    // monotone, so per axis the fraction inside the current cell is affine in
+    // the lane's iteration count: fr = fit * fst + fbs (one FMA). The ray
+    // leaves the cell when fr >= 1 (moving up) or fr <= 0 (moving down);
+    // then the next cell's {1/width, -c_k/width} is read (one float2) and
+    // fst/fbs are rebuilt. The cell record pointer q moves with the cell, so
+    // a sample is two 16-byte loads and the 7-FMA trilinear polynomial. The
+    // walk is confined to cells [-1, n-1] by the sentinel table entries, so
+    // every load is in bounds by construction.
     const CubeDev& C = *R.cube;
-    float st[3], bs[3], sg[3], iw[3], ncl[3], ncs[3];
-    const float4* cell[3];
+    float st[3], bs[3], fst[3], fbs[3], sg[3], cb[3];
+    const float2* cell[3];
     int dstr[3];
-    const float2* p00 = C.pv;
+    const float4* q = C.rec;  // record of the current cell (2 float4)
     if (iters > 0) {
-      long long off = (long long)C.pxy + C.px + 1;
-      const int stride[3] = {1, (int)C.px, (int)C.pxy};
+      int k0s[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const AxisDev& A = C.ax[k];
         st[k] = R.dt32 * d32[k] * fS;
         bs[k] = fmaf(fi, R.dt32 * d32[k], fmaf(0.5f, R.dt32 * d32[k], R.pos32[k]));
         sg[k] = d32[k] >= 0.f ? 1.f : -1.f;
+        cb[k] = d32[k] >= 0.f ? -1.f : 0.f;
         const float x0 = bs[k];
         float idx = A.uniform ? (x0 - A.c0) * A.inv_h : lut_index(A, C.lut, x0);
         int kb;
         magic_floor(fminf(fmaxf(idx, 0.f), (float)(A.n - 2)), kb);
         const int k0 = kb - kMagicBits;
         cell[k] = C.cells[k] + k0;
-        const float4 e = __ldg(cell[k]);
-        iw[k] = e.y;
-        ncl[k] = e.w;
-        ncs[k] = sg[k] > 0.f ? -e.z : e.x;
-        dstr[k] = sg[k] > 0.f ? stride[k] : -stride[k];
-        off += (long long)k0 * stride[k];
+        const float2 e = __ldg(cell[k]);
+        fst[k] = st[k] * e.x;
+        fbs[k] = fmaf(bs[k], e.x, e.y);
+        const int stride = (int)record_stride(C.cx, C.cxy, k);  // in records; 2 float4 each
+        dstr[k] = 2 * (sg[k] > 0.f ? stride : -stride);
+        k0s[k] = k0;
       }
-      p00 = C.pv + off;
+      q = C.rec + 2 * record_index(C.cx, C.cxy, k0s[0], k0s[1], k0s[2]);
     }
-    const float2* p01 = p00 + C.px;
-    const float2* p10 = p00 + C.pxy;
-    const float2* p11 = p10 + C.px;
-    // One sample at iteration fit: advance the cells (one branch for all
-    // three axes: the largest crossing test decides), then fetch and
-    // interpolate.
     auto sample = [&](float fit) -> float {
-      float x[3], cr[3], fr[3];
+      float fr[3], cr[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        x[k] = fmaf(fit, st[k], bs[k]);
-        cr[k] = fmaf(x[k], sg[k], ncs[k]);
+        fr[k] = fmaf(fit, fst[k], fbs[k]);
+        cr[k] = fmaf(fr[k], sg[k], cb[k]);  // >= 0: left the cell
       }
       if (fmaxf(fmaxf(cr[0], cr[1]), cr[2]) >= 0.f) {
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          // crossed the next node: step cells until x is inside (the
-          // sentinels end the walk at the box edge)
-          while (fmaf(x[k], sg[k], ncs[k]) >= 0.f) {
+          while (cr[k] >= 0.f) {
             cell[k] += (sg[k] > 0.f ? 1 : -1);
-            const float4 e = __ldg(cell[k]);
-            iw[k] = e.y;
-            ncl[k] = e.w;
-            ncs[k] = sg[k] > 0.f ? -e.z : e.x;
-            p00 += dstr[k];
-            p01 += dstr[k];
-            p10 += dstr[k];
-            p11 += dstr[k];
+            const float2 e = __ldg(cell[k]);
+            fst[k] = st[k] * e.x;
+            fbs[k] = fmaf(bs[k], e.x, e.y);
+            q += dstr[k];
+            fr[k] = fmaf(fit, fst[k], fbs[k]);
+            cr[k] = fmaf(fr[k], sg[k], cb[k]);
           }
         }
       }
-#pragma unroll
-      for (int k = 0; k < 3; ++k) fr[k] = fmaf(x[k], iw[k], ncl[k]);
-      const float2 c00 = __ldg(p00), c01 = __ldg(p01), c10 = __ldg(p10), c11 = __ldg(p11);
-      const float lx1 = lerp_f(c00.x, c00.y, fr[0]), lx2 = lerp_f(c01.x, c01.y, fr[0]);
-      const float hx1 = lerp_f(c10.x, c10.y, fr[0]), hx2 = lerp_f(c11.x, c11.y, fr[0]);
-      const float ly1 = lerp_f(lx1, lx2, fr[1]), hy1 = lerp_f(hx1, hx2, fr[1]);
-      return lerp_f(ly1, hy1, fr[2]);
+      const float4 lo = __ldg(q), hi = __ldg(q + 1);  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
+      const float b0 = fmaf(lo.y, fr[0], lo.x), a0 = fmaf(lo.w, fr[0], lo.z);
+      const float b1 = fmaf(hi.y, fr[0], hi.x), a1 = fmaf(hi.w, fr[0], hi.z);
+      return fmaf(fmaf(a1, fr[1], b1), fr[2], fmaf(a0, fr[1], b0));
     };
     // samples in pairs: the pair sum enters the compensated sum, halving the
     // serial Kahan chain
@@ -522,8 +511,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   } else if constexpr (KIND == SPACE_CUBE) {
     // nearest by truncation (UNIFORM / LUT index)
     const CubeDev& C = *R.cube;
-    const float* __restrict__ vals = reinterpret_cast<const float*>(C.pv);  // .x of pair i at 2i
-    const uint32_t px = C.px, pxy = C.pxy, bias = C.bias, max_off = C.max_off;
+    // node k's value is the first corner of cell k's record
+    const float* __restrict__ vals = reinterpret_cast<const float*>(C.rec);
+    const int cxn = (int)C.cx, cxyn = (int)C.cxy;
+    const int hi0 = C.ax[0].n - 1, hi1 = C.ax[1].n - 1, hi2 = C.ax[2].n - 1;
     float st[3], bs[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -583,9 +574,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           bz = cz + kMagicBits;
           if (stats) atomicAdd(&stats->exact_nearest, 1ull);
         }
-        uint32_t off = (uint32_t)bz * pxy + (uint32_t)by * px + (uint32_t)bx + bias;
-        off = min(off, max_off);
-        v = __ldg(vals + 2 * (size_t)off);
+        const int ix = min(max(bx - kMagicBits, -1), hi0), iy = min(max(by - kMagicBits, -1), hi1),
+                  iz = min(max(bz - kMagicBits, -1), hi2);
+        v = __ldg(vals + 8 * record_index(cxn, cxyn, ix, iy, iz));
       }
       acc.add(v);
       fi += fS;
@@ -726,11 +717,26 @@ __global__ void cube_guard_kernel(float* dst, int nx, int ny, int nz) {
   }
 }
 
-// Pair grid from the padded scalar grid: pair i = {v[i], v[i+1]} (the last
-// node of each row is never the left corner of a cell).
-__global__ void cube_pairs_kernel(const float* __restrict__ v, size_t total, float2* __restrict__ out) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = make_float2(v[i], v[i + 1 < total ? i + 1 : i]);
+// Cell records from the padded scalar grid ((nx+2)(ny+2)(nz+2), node i at
+// padded index i+1): record (a, b, c), a in [0, nx], is the trilinear
+// polynomial of the 8 padded nodes (a..a+1, b..b+1, c..c+1) (cell a-1 of the
+// unpadded grid), coefficients computed in FP64 and rounded once.
+__global__ void cube_records_kernel(const float* __restrict__ v, int nx, int ny, int nz, float4* __restrict__ rec) {
+  const long long cx = nx + 1, cy = ny + 1, cz = nz + 1, px = nx + 2, pxy = (long long)(nx + 2) * (ny + 2);
+  const long long n = cx * cy * cz;
+  for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+    const long long a = r % cx, b = (r / cx) % cy, c = r / (cx * cy);
+    const float* p = v + c * pxy + b * px + a;
+    const double v000 = p[0], v001 = p[1], v010 = p[px], v011 = p[px + 1];
+    const double v100 = p[pxy], v101 = p[pxy + 1], v110 = p[pxy + px], v111 = p[pxy + px + 1];
+    const double c1 = v001 - v000, c2 = v010 - v000, c3 = v100 - v000;
+    const double c4 = (v011 - v010) - (v001 - v000);
+    const double c5 = (v101 - v100) - (v001 - v000);
+    const double c6 = (v110 - v100) - (v010 - v000);
+    const double c7 = ((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000));
+    rec[2 * r] = make_float4((float)v000, (float)c1, (float)c2, (float)c4);
+    rec[2 * r + 1] = make_float4((float)c3, (float)c5, (float)c6, (float)c7);
+  }
 }
 
 // DataCube::GetSample for a batch of points: exact FP64 in-box test and cell
@@ -762,15 +768,16 @@ __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int triline
       out[t] = -1.f;
       continue;
     }
-    const float2* b = C.pv + ((size_t)(k[2] + 1) * C.pxy + (size_t)(k[1] + 1) * C.px + (k[0] + 1));
+    const float4* b = C.rec + 2 * record_index(C.cx, C.cxy, k[0], k[1], k[2]);
+    const float4 lo = b[0], hi = b[1];  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
     if (!trilinear) {
-      out[t] = b[0].x;
+      out[t] = lo.x;
       continue;
     }
-    auto L = [](double u, double v, double w) { return u + w * (v - u); };
-    double lx1 = L(b[0].x, b[0].y, f[0]), lx2 = L(b[C.px].x, b[C.px].y, f[0]);
-    double hx1 = L(b[C.pxy].x, b[C.pxy].y, f[0]), hx2 = L(b[C.pxy + C.px].x, b[C.pxy + C.px].y, f[0]);
-    out[t] = (float)L(L(lx1, lx2, f[1]), L(hx1, hx2, f[1]), f[2]);
+    const double x = f[0], y = f[1], z = f[2];
+    const double bot = (double)lo.x + x * lo.y + y * ((double)lo.z + x * lo.w);
+    const double top = (double)hi.x + x * hi.y + y * ((double)hi.z + x * hi.w);
+    out[t] = (float)(bot + z * top);
   }
 }
 
@@ -896,9 +903,10 @@ cudaError_t launch_cube_fill(const float*, int nx, int ny, int nz, float* dst, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_cube_pairs(const float* padded, size_t total, float2* pairs, cudaStream_t s) {
-  int blocks = (int)std::min<size_t>((total + 255) / 256, 8192);
-  cube_pairs_kernel<<<blocks, 256, 0, s>>>(padded, total, pairs);
+cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, float4* rec, cudaStream_t s) {
+  const long long n = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+  int blocks = (int)std::min<long long>((n + 255) / 256, 8192);
+  cube_records_kernel<<<blocks, 256, 0, s>>>(padded, nx, ny, nz, rec);
   return cudaGetLastError();
 }
 

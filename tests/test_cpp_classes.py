@@ -68,3 +68,14 @@ def test_classes_on_gpu(tmp_path, birp, oracle):
     m = ref > 1e-3 * ref.max()
     assert (np.abs(img[m] - ref[m]) / ref[m]).max() <= 1e-5
     assert np.float32(cards["POS_X"]) == np.float32(5.91813)  # 9 digits round-trip FP32
+
+
+def test_cell_record_index_arithmetic(tmp_path):
+    """The record addressing the kernels share (csrc/cell_index.h), checked on
+    the host: in range for cells -1..n-1, equal to the build order, and kept
+    in range by unit steps."""
+    exe = str(tmp_path / "cell_index_test")
+    subprocess.run(["g++", "-O2", "-std=c++17", os.path.join(ROOT, "tests", "cpp", "cell_index_test.cpp"), "-o", exe],
+                   check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
