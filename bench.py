@@ -38,8 +38,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "images/s & p99 latency: batched/served vs plain GPU render at ≤1e-5 rel err"
 UNIT = "images/s"
-FLOP_PER_SAMPLE = 40.0   # trilinear ray-sample: 6 position + 6 index + 3 frac + 21 lerp + 4 Kahan
-BYTES_PER_SAMPLE = 32.0  # 8 FP32 corners gathered
+# Per trilinear ray-sample (the reference's formulation): 8 FP32 corners
+# gathered, 6 position + 6 index + 3 fraction + 21 lerp + 4 Kahan flops.
+FLOP_PER_SAMPLE = 40.0
+BYTES_PER_SAMPLE = 32.0
+# Per cell segment (what the kernel does: the samples inside one cell summed
+# in closed form): one 32-byte coefficient record + one 16-byte axis-table
+# entry for the step into the cell; ~72 flops for the closed-form sum and
+# Kahan update plus ~7 for the exit index of the stepped axis.
+FLOP_PER_CELL = 80.0
+BYTES_PER_CELL = 48.0
 
 
 def dist_setup():
@@ -458,20 +466,28 @@ def main():
     # ---- roofline of the batched kernel (measured peaks)
     fp32_tflops, l2_gbs = B.measure_peaks()
     t_k = step_ms / 1000.0
-    achieved_flops = samples_per_step * FLOP_PER_SAMPLE / t_k / 1e12
-    achieved_bytes = samples_per_step * BYTES_PER_SAMPLE / t_k / 1e9
-    t_flop = samples_per_step * FLOP_PER_SAMPLE / (fp32_tflops * 1e12)
-    t_byte = samples_per_step * BYTES_PER_SAMPLE / (l2_gbs * 1e9)
-    if t_flop >= t_byte:
-        roofline = {"bound": "fp32", "achieved": achieved_flops, "peak": fp32_tflops, "unit": "TFLOP/s",
-                    "frac": achieved_flops / fp32_tflops}
-    else:
-        roofline = {"bound": "l2", "achieved": achieved_bytes, "peak": l2_gbs, "unit": "GB/s",
-                    "frac": achieved_bytes / l2_gbs}
+    cells_per_step = ks["cells"] / args.steps
+
+    def roof(units, flop_per, bytes_per, label):
+        af = units * flop_per / t_k / 1e12
+        ab = units * bytes_per / t_k / 1e9
+        if units * flop_per / (fp32_tflops * 1e12) >= units * bytes_per / (l2_gbs * 1e9):
+            r = {"bound": "fp32", "achieved": af, "peak": fp32_tflops, "unit": "TFLOP/s", "frac": af / fp32_tflops}
+        else:
+            r = {"bound": "l2", "achieved": ab, "peak": l2_gbs, "unit": "GB/s", "frac": ab / l2_gbs}
+        r["units"] = label
+        return r
+
+    roofline = roof(cells_per_step, FLOP_PER_CELL, BYTES_PER_CELL,
+                    f"{cells_per_step:.4g} cell segments/launch x {FLOP_PER_CELL:.0f} flop, {BYTES_PER_CELL:.0f} B")
     roofline.update({"traffic": traffic_from_profile(), "kernel": "render_batch_kernel",
                      "peak_source": "measured in-run: FP32 FMA loop and L2-resident read (birp_measure_peaks)",
-                     "units": f"{samples_per_step:.4g} ray-samples/launch x {FLOP_PER_SAMPLE:.0f} flop, "
-                              f"{BYTES_PER_SAMPLE:.0f} B gathered"})
+                     "fp32_frac": cells_per_step * FLOP_PER_CELL / t_k / 1e12 / fp32_tflops,
+                     "l2_frac": cells_per_step * BYTES_PER_CELL / t_k / 1e9 / l2_gbs})
+    roofline_per_sample = roof(samples_per_step, FLOP_PER_SAMPLE, BYTES_PER_SAMPLE,
+                               f"{samples_per_step:.4g} ray-samples/launch x {FLOP_PER_SAMPLE:.0f} flop, "
+                               f"{BYTES_PER_SAMPLE:.0f} B (per-sample formulation; the kernel sums "
+                               f"{samples_per_step / max(cells_per_step, 1):.2f} samples per cell in closed form)")
     peaks_file = os.path.join(ROOT, "MEASURED_PEAKS.json")
     hbm = None
     if os.path.exists(peaks_file):
@@ -507,10 +523,11 @@ def main():
             "e2e_vs_plain": (e2e / plain) if plain else None,
             "serving": serving,
             "ray_samples_per_s": samples_per_step * world / (step_ms / 1000.0),
-            "roofline": roofline, "roofline_hbm": roofline_hbm,
+            "roofline": roofline, "roofline_per_sample": roofline_per_sample, "roofline_hbm": roofline_hbm,
             "cpu_baseline": cpu, "parity": parity,
             "gpu_launches": args.steps, "clocks": clocks.summary(),
             "exact_fp64_rays_per_step": ks["exact_range_rays"] / args.steps,
+            "samples_per_cell": (ks["samples"] / ks["cells"]) if ks.get("cells") else None,
         }
         print(json.dumps(line))
 

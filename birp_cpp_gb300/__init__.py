@@ -65,7 +65,8 @@ class ServerStats(C.Structure):
 
 
 class KernelStats(C.Structure):
-    _fields_ = [(n, C.c_uint64) for n in ("exact_range_rays", "exact_nearest", "exact_cmem", "items", "samples")]
+    _fields_ = [(n, C.c_uint64) for n in ("exact_range_rays", "exact_nearest", "exact_cmem", "items", "samples",
+                                          "cells")]
 
 
 _lib = None

@@ -44,11 +44,12 @@ struct CubeDev {
   uint32_t cxy;         // records per z slab: (nx + 1) * (ny + 1)
   int all_uniform;
   const float4* lut;    // concatenated LUT bins (nullptr if all uniform)
-  // per axis, per cell k in [0, n-2]: {1/(c_{k+1}-c_k), -c_k/(c_{k+1}-c_k)} in
-  // FP32 (the cell fraction is x * first + second), for marching cell by cell
-  // along a ray; entries -1 and n-1 are sentinels {0, 1} and {0, 0} whose
-  // fraction never leaves [0, 1], which stops the march at the box edge
-  const float2* cells[3];
+  // per axis, per cell k in [0, n-2]: {1/w_k, -c_k/w_k, w_k, 0} in FP32 with
+  // w_k = c_{k+1} - c_k (the cell fraction is x * .x + .y), for marching cell
+  // by cell along a ray; entries -1 and n-1 are sentinels {0, 1, inf, 0} and
+  // {0, 0, inf, 0} whose fraction never changes, which stops the march at the
+  // box edge
+  const float4* cells[3];
 };
 
 // CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
@@ -94,6 +95,7 @@ struct KernelStats {
   unsigned long long exact_cmem;         // CMEM samples decided in FP64
   unsigned long long items;              // work items rendered (persistent kernel)
   unsigned long long samples;            // ray-samples evaluated
+  unsigned long long cells;              // cell segments integrated (cell-space march)
   unsigned int error;                    // nonzero: a device-side consistency check failed
   unsigned int error_info;
 };

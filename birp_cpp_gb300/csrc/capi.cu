@@ -553,6 +553,7 @@ birp_status birp_get_kernel_stats(birp_kernel_stats* out, int reset) {
   out->exact_cmem = k.exact_cmem;
   out->items = k.items;
   out->samples = k.samples;
+  out->cells = k.cells;
   if (reset) CK(cudaMemset(g_ctx.stats, 0, sizeof(KernelStats)));
   if (k.error) return fail(BIRP_ERR_DEVICE, "device check %u failed (info %u)", k.error, k.error_info);
   return ok();

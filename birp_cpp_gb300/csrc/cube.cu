@@ -136,24 +136,26 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   }
 
   size_t coords = (size_t)nx + ny + nz;
-  // per-cell march table of every axis: cells 0..n-2 between two sentinels
-  // (iw = 0, fraction fixed at 1 below and 0 above: the walk stops there; a
-  // cell pointer cannot leave [-1, n-1], whose records all exist)
-  std::vector<float2> cells;
+  // per-cell march table of every axis: {1/width, -c_k/width, width, 0} for
+  // cells 0..n-2 between two sentinels {0, 1, inf, 0} / {0, 0, inf, 0} whose
+  // fraction never changes (the walk stops there; a cell pointer cannot leave
+  // [-1, n-1], whose records all exist)
+  std::vector<float4> cells;
   cells.reserve(coords + 3);
   size_t cell_off[3];
   for (int k = 0; k < 3; ++k) {
     const std::vector<double>& ck = c.c[k];
     const int n = c.n[k];
-    cells.push_back(make_float2(0.f, 1.f));
+    cells.push_back(make_float4(0.f, 1.f, INFINITY, 0.f));
     cell_off[k] = cells.size();
     for (int i = 0; i + 1 < n; ++i) {
-      double iw = 1.0 / (ck[i + 1] - ck[i]);
-      cells.push_back(make_float2((float)iw, (float)(-ck[i] * iw)));
+      double w = ck[i + 1] - ck[i];
+      double iw = 1.0 / w;
+      cells.push_back(make_float4((float)iw, (float)(-ck[i] * iw), (float)w, 0.f));
     }
-    cells.push_back(make_float2(0.f, 0.f));
+    cells.push_back(make_float4(0.f, 0.f, INFINITY, 0.f));
   }
-  CKU(dev_alloc(&c.d_cells, cells.size() * sizeof(float2), c.alloc_stream));
+  CKU(dev_alloc(&c.d_cells, cells.size() * sizeof(float4), c.alloc_stream));
   const size_t records = ((size_t)nx + 1) * ((size_t)ny + 1) * ((size_t)nz + 1);
   CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
   float* scalar = nullptr;  // the padded scalar grid, turned into cell records then freed
@@ -162,7 +164,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   if (!lut.empty()) CKU(dev_alloc(&c.d_lut, lut.size() * sizeof(float4), c.alloc_stream));
   CKU(dev_alloc(&c.d_desc, sizeof(CubeDev), c.alloc_stream));
   c.device_bytes = records * 2 * sizeof(float4) + coords * sizeof(double) + lut.size() * sizeof(float4) +
-                   cells.size() * sizeof(float2) +
+                   cells.size() * sizeof(float4) +
                    sizeof(CubeDev);
 
   // interior values: one strided 3D copy from the caller's x-fastest array
@@ -184,7 +186,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   for (int k = 0; k < 3; ++k) all.insert(all.end(), c.c[k].begin(), c.c[k].end());
   CKU(cudaMemcpyAsync(c.d_c64, all.data(), coords * sizeof(double), cudaMemcpyHostToDevice, st));
   if (!lut.empty()) CKU(cudaMemcpyAsync(c.d_lut, lut.data(), lut.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CKU(cudaMemcpyAsync(c.d_cells, cells.data(), cells.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+  CKU(cudaMemcpyAsync(c.d_cells, cells.data(), cells.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
 
   size_t off = 0;
   for (int k = 0; k < 3; ++k) {
@@ -225,7 +227,7 @@ size_t cube_device_bytes(const birp_cube& c) {
   if (!all_uniform)
     for (int k = 0; k < 3; ++k)
       lut += (size_t)std::max(1.0, std::ceil((c.c[k].back() - c.c[k].front()) / c.min_gap[k])) * sizeof(float4);
-  const size_t cells = (coords + 3) * sizeof(float2);
+  const size_t cells = (coords + 3) * sizeof(float4);
   const size_t records = ((size_t)c.n[0] + 1) * ((size_t)c.n[1] + 1) * ((size_t)c.n[2] + 1);
   return records * 2 * sizeof(float4) + coords * sizeof(double) + lut + cells + sizeof(CubeDev);
 }

@@ -18,8 +18,10 @@
 //    in FP64 only when the bound cannot decide), nearest-cell choices within
 //    the bound of a node, and CMEM shell choices within the bound of a
 //    discontinuity.
-//  * Cube values are FP32 in HBM with a guard layer (birp_internal.h); the
-//    8 corners of a cell are fetched through the read-only path; the FP32
+//  * A cube is stored as one 32-byte record of trilinear coefficients per
+//    cell (birp_internal.h). The trilinear march walks a ray cell by cell and
+//    sums each cell's samples in closed form (a cubic in the sample index),
+//    so it reads one record per cell, not 8 corners per sample. The FP32
 //    floor uses the magic-constant trick (no conversion-pipe instructions).
 #include <algorithm>
 #include <cstdint>
@@ -159,7 +161,9 @@ __device__ __forceinline__ AxisEst axis_range_fast(float p, float d, float blo, 
   float inv = 1.0f / (d * dt);
   float ul = fmaf(blo - p, inv, -0.5f);
   float uh = fmaf(bhi - p, inv, -0.5f);
-  float rel = kDirErr / ad + 1e-6f;
+  // direction error, plus the FP32 rounding of u itself (the difference,
+  // the reciprocal of d*dt and the fused multiply-add: <= 2.4e-7 relative)
+  float rel = kDirErr / ad + 4e-7f;
   float ainv = fabsf(inv);
   float el = (fabsf(ul) + 1.f) * rel + (fabsf(blo) + fabsf(p)) * 2.4e-7f * ainv + 1e-5f;
   float eh = (fabsf(uh) + 1.f) * rel + (fabsf(bhi) + fabsf(p)) * 2.4e-7f * ainv + 1e-5f;
@@ -432,82 +436,112 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   float fi = (float)first;
   const float fS = (float)S;
 
+  int nsamp = iters;  // samples this lane evaluates (for the counters)
   if constexpr (KIND == SPACE_CUBE && AXES == AXES_DDA) {
-    // Cell-by-cell march in fraction space. Along a ray each coordinate is
-    // monotone, so per axis the fraction inside the current cell is affine in
-    // the lane's iteration count: fr = fit * fst + fbs (one FMA). The ray
-    // leaves the cell when fr >= 1 (moving up) or fr <= 0 (moving down);
-    // then the next cell's {1/width, -c_k/width} is read (one float2) and
-    // fst/fbs are rebuilt. The cell record pointer q moves with the cell, so
-    // a sample is two 16-byte loads and the 7-FMA trilinear polynomial. The
-    // walk is confined to cells [-1, n-1] by the sentinel table entries, so
-    // every load is in bounds by construction.
+    // Cell-space integration. A lane takes a contiguous run of its ray's
+    // samples and walks the cells the run crosses. Per axis the cell fraction
+    // is affine in the sample index u (fr = fbs + u * fst) and the ray leaves
+    // the cell at u = E (fr reaches 1 moving up, 0 moving down). Within one
+    // cell the trilinear polynomial along the ray is a cubic in u, so the
+    // sum over the m samples in the cell is a0 m + a1 S1 + a2 S2 + a3 S3 with
+    // the power sums S_p = sum_{j<m} j^p and a_p the cubic's coefficients at
+    // the cell's first sample: one 32-byte record and ~30 FMAs per cell
+    // instead of per sample. Sample counts are exact integers and the field
+    // is continuous across cell faces, so a sample on a face may go to either
+    // cell. The walk is confined to cells [-1, n-1] by the sentinel table
+    // entries, so every load is in bounds by construction; the loop is also
+    // capped at (samples + cells + 4) steps.
     const CubeDev& C = *R.cube;
-    float st[3], bs[3], fst[3], fbs[3], sg[3], cb[3];
-    const float2* cell[3];
+    const int total = b - a;
+    const int seglen = (total + S - 1) >> SEGL2;
+    const int first_c = a + min(seg * seglen, total);
+    const int count = max(0, min(total - seg * seglen, seglen));
+    nsamp = count;
+    // per axis: position step st, its reciprocal, position at the run's first
+    // sample, the current cell's fraction slope/intercept and exit index, the
+    // direction sg, the exit side tk (1 moving up, 0 down) and the record step
+    float st[3], rst[3], bs[3], fst[3], fbs[3], ex[3], tk[3], sg[3];
+    const float4* cell[3];
     int dstr[3];
-    const float4* q = C.rec;  // record of the current cell (2 float4)
-    if (iters > 0) {
+    const float4* q = C.rec;
+    if (count > 0) {
+      const float f0 = (float)first_c;
       int k0s[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const AxisDev& A = C.ax[k];
-        st[k] = R.dt32 * d32[k] * fS;
-        bs[k] = fmaf(fi, R.dt32 * d32[k], fmaf(0.5f, R.dt32 * d32[k], R.pos32[k]));
-        sg[k] = d32[k] >= 0.f ? 1.f : -1.f;
-        cb[k] = d32[k] >= 0.f ? -1.f : 0.f;
-        const float x0 = bs[k];
-        float idx = A.uniform ? (x0 - A.c0) * A.inv_h : lut_index(A, C.lut, x0);
+        st[k] = R.dt32 * d32[k];
+        rst[k] = 1.0f / st[k];  // samples per unit length along the axis (inf if d = 0)
+        bs[k] = fmaf(f0, st[k], fmaf(0.5f, st[k], R.pos32[k]));
+        // direction from the sign bit, so that a zero step of either sign
+        // (rst = +-inf) gives an exit index of +inf (or NaN), never a crossing
+        sg[k] = signbit(d32[k]) ? -1.f : 1.f;
+        tk[k] = signbit(d32[k]) ? 0.f : 1.f;
+        float idx = A.uniform ? (bs[k] - A.c0) * A.inv_h : lut_index(A, C.lut, bs[k]);
         int kb;
         magic_floor(fminf(fmaxf(idx, 0.f), (float)(A.n - 2)), kb);
-        const int k0 = kb - kMagicBits;
-        cell[k] = C.cells[k] + k0;
-        const float2 e = __ldg(cell[k]);
+        k0s[k] = kb - kMagicBits;
+        cell[k] = C.cells[k] + k0s[k];
+        const float4 e = __ldg(cell[k]);
         fst[k] = st[k] * e.x;
         fbs[k] = fmaf(bs[k], e.x, e.y);
-        const int stride = (int)record_stride(C.cx, C.cxy, k);  // in records; 2 float4 each
+        // exit index of the cell along this axis: (tk - fr(0)) / fst =
+        // (tk - fbs) * w / st (NaN at a sentinel, whose width is inf, and +inf
+        // when the axis is not crossed)
+        ex[k] = (tk[k] - fbs[k]) * (rst[k] * e.z);
+        const int stride = (int)record_stride(C.cx, C.cxy, k);
         dstr[k] = 2 * (sg[k] > 0.f ? stride : -stride);
-        k0s[k] = k0;
       }
       q = C.rec + 2 * record_index(C.cx, C.cxy, k0s[0], k0s[1], k0s[2]);
-    }
-    auto sample = [&](float fit) -> float {
-      float fr[3], cr[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        fr[k] = fmaf(fit, fst[k], fbs[k]);
-        cr[k] = fmaf(fr[k], sg[k], cb[k]);  // >= 0: left the cell
-      }
-      if (fmaxf(fmaxf(cr[0], cr[1]), cr[2]) >= 0.f) {
+      const float ub = (float)count;
+      float u = 0.f;
+      const int cap = count + C.ax[0].n + C.ax[1].n + C.ax[2].n + 4;
+      int ncell = 0;
+      for (int guard = 0; u < ub && guard < cap; ++guard) {
+        const float4 lo = __ldg(q), hi = __ldg(q + 1);  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
+        const float nxt = fminf(ceilf(fminf(fminf(ex[0], ex[1]), ex[2])), ub);
+        if (nxt > u) {
+          const float m = nxt - u;
+          const float X = fmaf(u, fst[0], fbs[0]), Y = fmaf(u, fst[1], fbs[1]), Z = fmaf(u, fst[2], fbs[2]);
+          const float Dx = fst[0], Dy = fst[1], Dz = fst[2];
+          // value, gradient and mixed second derivatives at the first sample
+          const float b0 = fmaf(lo.y, X, lo.x);  // c0 + c1 X
+          const float a0 = fmaf(lo.w, X, lo.z);  // c2 + c4 X
+          const float b1 = fmaf(hi.y, X, hi.x);  // c3 + c5 X
+          const float a1 = fmaf(hi.w, X, hi.z);  // c6 + c7 X  (= f_yz)
+          const float lowz = fmaf(a0, Y, b0), gz = fmaf(a1, Y, b1);
+          const float f0v = fmaf(gz, Z, lowz);
+          const float gy = fmaf(a1, Z, a0);
+          const float hxy = fmaf(hi.w, Z, lo.w), hxz = fmaf(hi.w, Y, hi.y);  // c4 + c7 Z, c5 + c7 Y
+          const float gx = fmaf(hxz, Z, fmaf(lo.w, Y, lo.y));  // c1 + c4 Y + c5 Z + c7 Y Z
+          const float p1 = fmaf(gx, Dx, fmaf(gy, Dy, gz * Dz));
+          const float DxDy = Dx * Dy;
+          const float p2 = fmaf(hxy, DxDy, fmaf(hxz, Dx * Dz, a1 * (Dy * Dz)));
+          const float p3 = hi.w * (DxDy * Dz);
+          const float mm1 = m * (m - 1.f);
+          const float s1 = 0.5f * mm1;
+          const float s2 = mm1 * (2.f * m - 1.f) * (1.f / 6.f);
+          const float s3 = s1 * s1;
+          acc.add(fmaf(p3, s3, fmaf(p2, s2, fmaf(p1, s1, f0v * m))));
+          u = nxt;
+          ++ncell;
+        }
+        // step every axis whose exit index has been reached; the sentinel's
+        // exit index is NaN, which ends the loop at the table's end
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-          while (cr[k] >= 0.f) {
+          while (ex[k] <= u) {
             cell[k] += (sg[k] > 0.f ? 1 : -1);
-            const float2 e = __ldg(cell[k]);
-            fst[k] = st[k] * e.x;
-            fbs[k] = fmaf(bs[k], e.x, e.y);
+            const float4 en = __ldg(cell[k]);
+            fst[k] = st[k] * en.x;
+            fbs[k] = fmaf(bs[k], en.x, en.y);
+            ex[k] = (tk[k] - fbs[k]) * (rst[k] * en.z);
             q += dstr[k];
-            fr[k] = fmaf(fit, fst[k], fbs[k]);
-            cr[k] = fmaf(fr[k], sg[k], cb[k]);
           }
         }
       }
-      const float4 lo = __ldg(q), hi = __ldg(q + 1);  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
-      const float b0 = fmaf(lo.y, fr[0], lo.x), a0 = fmaf(lo.w, fr[0], lo.z);
-      const float b1 = fmaf(hi.y, fr[0], hi.x), a1 = fmaf(hi.w, fr[0], hi.z);
-      return fmaf(fmaf(a1, fr[1], b1), fr[2], fmaf(a0, fr[1], b0));
-    };
-    // samples in pairs: the pair sum enters the compensated sum, halving the
-    // serial Kahan chain
-    float fit = 0.f;  // iteration count as float (no conversion per sample)
-    int it = 0;
-    for (; it + 1 < iters; it += 2) {
-      const float va = sample(fit);
-      const float vb = sample(fit + 1.f);
-      acc.add(va + vb);
-      fit += 2.f;
+      if (stats) atomicAdd(&stats->cells, (unsigned long long)ncell);
     }
-    if (it < iters) acc.add(sample(fit));
   } else if constexpr (KIND == SPACE_CUBE) {
     // nearest by truncation (UNIFORM / LUT index)
     const CubeDev& C = *R.cube;
@@ -611,7 +645,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   }
 
   if (stats) {
-    unsigned int cnt = __reduce_add_sync(0xffffffffu, (unsigned int)iters);
+    unsigned int cnt = __reduce_add_sync(0xffffffffu, (unsigned int)nsamp);
     if (lane == 0 && cnt) atomicAdd(&stats->samples, (unsigned long long)cnt);
   }
   // merge the S partial sums of a ray

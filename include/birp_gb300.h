@@ -242,6 +242,7 @@ typedef struct {
   uint64_t exact_cmem;         /* CMEM samples decided in FP64 */
   uint64_t items;              /* tiles rendered by the persistent kernel */
   uint64_t samples;            /* ray-samples evaluated (the roofline's unit) */
+  uint64_t cells;              /* cell segments integrated by the trilinear march */
 } birp_kernel_stats;
 
 /* Reads (and optionally clears) the kernels' counters. */

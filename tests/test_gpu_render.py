@@ -282,4 +282,4 @@ def test_edge_cases(birp, oracle):
 
 def test_kernel_stats_readable(birp):
     s = birp.kernel_stats(reset=True)
-    assert set(s) == {"exact_range_rays", "exact_nearest", "exact_cmem", "items", "samples"}
+    assert set(s) == {"exact_range_rays", "exact_nearest", "exact_cmem", "items", "samples", "cells"}
