@@ -43,11 +43,12 @@ UNIT = "images/s"
 FLOP_PER_SAMPLE = 40.0
 BYTES_PER_SAMPLE = 32.0
 # Per cell segment (what the kernel does: the samples inside one cell summed
-# in closed form): one 32-byte coefficient record + one 16-byte axis-table
-# entry for the step into the cell; ~72 flops for the closed-form sum and
-# Kahan update plus ~7 for the exit index of the stepped axis.
-FLOP_PER_CELL = 80.0
-BYTES_PER_CELL = 48.0
+# in closed form): one 32-byte coefficient record + one 8-byte walk-table
+# entry for the face crossed into the cell; 65 FP32 operations for the run
+# end, the closed-form sum and the Kahan update (FMA = 2) plus 3 for the new
+# base offset and exit index of the crossed axis.
+FLOP_PER_CELL = 68.0
+BYTES_PER_CELL = 40.0
 
 
 def dist_setup():

@@ -21,7 +21,7 @@ struct birp_cube {
   float4* d_vals = nullptr;     // cell records (birp_internal.h)
   double* d_c64 = nullptr;      // 3 axes, concatenated
   float4* d_lut = nullptr;
-  float4* d_cells = nullptr;    // per-cell march tables, 3 axes concatenated
+  float2* d_cells = nullptr;    // walk tables (up and down) of the 3 axes, concatenated
   size_t device_bytes = 0;
   cudaStream_t alloc_stream = nullptr;  // non-null: stream-ordered (pool) allocations
 };

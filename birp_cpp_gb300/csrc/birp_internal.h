@@ -2,15 +2,21 @@
 //
 // Data layout in HBM (one cube):
 //  * values: one 32-byte record per cell holding the 8 coefficients of its
-//    trilinear polynomial f(x,y,z) = c0 + c1 x + c2 y + c3 z + c4 xy + c5 xz
-//    + c6 yz + c7 xyz (x, y, z the cell fractions), computed in FP64 from the
-//    FP32 corner values and stored FP32 as {c0, c1, c2, c4 | c3, c5, c6, c7};
-//    c0 is the value of the cell's lower corner (node k). Records are x
-//    fastest for cells -1..n-1 on every axis (one guard cell each side whose
-//    outside corners repeat the edge node), so a cell index that FP32
-//    rounding puts one step outside [0, n-2] still reads in-bounds memory and
-//    interpolates continuously. A sample is two 16-byte loads from one
-//    pointer and 7 FMAs.
+//    trilinear polynomial f = c0 + c1 x + c2 y + c3 z + c4 xy + c5 xz + c6 yz
+//    + c7 xyz in the cell's local coordinates (x, y, z) = p - (lower node)
+//    (physical units, so a ray's step along an axis is the same in every
+//    cell), computed in FP64 from the FP32 corner values and stored FP32 as
+//    {c0, c1, c2, c4 | c3, c5, c6, c7}; c0 is the value of the cell's lower
+//    corner (node k). Records are x fastest for cells -1..n-1 on every axis:
+//    one guard cell each side whose outside corners repeat the edge node and
+//    whose coefficients along that axis are exactly 0, so a cell index that
+//    FP32 rounding puts one step outside [0, n-2] still reads in-bounds
+//    memory and interpolates continuously.
+//  * per-axis walk tables: float2 {base, exit plane} per cell -1..n-1, one
+//    table for rays moving up (exit plane c_{k+1}) and one, stored in reverse
+//    cell order, for rays moving down (exit plane c_k), so a ray always walks
+//    its table forward. The guard cells' exit planes are +inf / -inf, which
+//    ends the walk at the box edge.
 //  * per-axis index tables (LUT) for nonuniform axes: float4 bins of width at
 //    most the smallest cell, each holding one piecewise-linear index map.
 //  * FP64 axis coordinates, read only by the exact (FP64) decisions.
@@ -44,12 +50,10 @@ struct CubeDev {
   uint32_t cxy;         // records per z slab: (nx + 1) * (ny + 1)
   int all_uniform;
   const float4* lut;    // concatenated LUT bins (nullptr if all uniform)
-  // per axis, per cell k in [0, n-2]: {1/w_k, -c_k/w_k, w_k, 0} in FP32 with
-  // w_k = c_{k+1} - c_k (the cell fraction is x * .x + .y), for marching cell
-  // by cell along a ray; entries -1 and n-1 are sentinels {0, 1, inf, 0} and
-  // {0, 0, inf, 0} whose fraction never changes, which stops the march at the
-  // box edge
-  const float4* cells[3];
+  // walk tables (see above): walk_up[k] + j and walk_dn[k] - j are cell j's
+  // entries, j in [-1, n-1]
+  const float2* walk_up[3];
+  const float2* walk_dn[3];
 };
 
 // CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
@@ -120,7 +124,8 @@ enum BatchClass : int { BATCH_CUBE_TRI = 0, BATCH_ANY = 1 };
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
-cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, float4* rec, cudaStream_t stream);
+cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, const double* cx64, const double* cy64,
+                                const double* cz64, float4* rec, cudaStream_t stream);
 cudaError_t launch_cube_sample(const CubeDev* cube, int trilinear, const float* xyz, int n, float* out,
                                cudaStream_t stream);
 cudaError_t launch_cmem_sample(const CmemDev* cmem, const float* xyz, int n, float* out, cudaStream_t stream);

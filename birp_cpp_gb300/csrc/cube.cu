@@ -136,26 +136,26 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   }
 
   size_t coords = (size_t)nx + ny + nz;
-  // per-cell march table of every axis: {1/width, -c_k/width, width, 0} for
-  // cells 0..n-2 between two sentinels {0, 1, inf, 0} / {0, 0, inf, 0} whose
-  // fraction never changes (the walk stops there; a cell pointer cannot leave
-  // [-1, n-1], whose records all exist)
-  std::vector<float4> cells;
-  cells.reserve(coords + 3);
-  size_t cell_off[3];
+  // walk tables of every axis, {base, exit plane} per cell -1..n-1: the up
+  // table in cell order, then the down table in reverse cell order. Guard
+  // cells take the edge node as base (their coefficients along the axis are
+  // 0) and an infinite exit plane, so the walk stops there.
+  std::vector<float2> walk;
+  walk.reserve(2 * (coords + 3));
+  size_t up_off[3], dn_off[3];
   for (int k = 0; k < 3; ++k) {
     const std::vector<double>& ck = c.c[k];
     const int n = c.n[k];
-    cells.push_back(make_float4(0.f, 1.f, INFINITY, 0.f));
-    cell_off[k] = cells.size();
-    for (int i = 0; i + 1 < n; ++i) {
-      double w = ck[i + 1] - ck[i];
-      double iw = 1.0 / w;
-      cells.push_back(make_float4((float)iw, (float)(-ck[i] * iw), (float)w, 0.f));
-    }
-    cells.push_back(make_float4(0.f, 0.f, INFINITY, 0.f));
+    walk.push_back(make_float2((float)ck[0], (float)ck[0]));  // cell -1
+    up_off[k] = walk.size();
+    for (int j = 0; j + 1 < n; ++j) walk.push_back(make_float2((float)ck[j], (float)ck[j + 1]));
+    walk.push_back(make_float2((float)ck[n - 1], INFINITY));  // cell n-1
+    walk.push_back(make_float2((float)ck[n - 1], (float)ck[n - 1]));  // cell n-1
+    for (int j = n - 2; j >= 0; --j) walk.push_back(make_float2((float)ck[j], (float)ck[j]));
+    dn_off[k] = walk.size() - 1;  // cell 0
+    walk.push_back(make_float2((float)ck[0], -INFINITY));  // cell -1
   }
-  CKU(dev_alloc(&c.d_cells, cells.size() * sizeof(float4), c.alloc_stream));
+  CKU(dev_alloc(&c.d_cells, walk.size() * sizeof(float2), c.alloc_stream));
   const size_t records = ((size_t)nx + 1) * ((size_t)ny + 1) * ((size_t)nz + 1);
   CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
   float* scalar = nullptr;  // the padded scalar grid, turned into cell records then freed
@@ -164,7 +164,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   if (!lut.empty()) CKU(dev_alloc(&c.d_lut, lut.size() * sizeof(float4), c.alloc_stream));
   CKU(dev_alloc(&c.d_desc, sizeof(CubeDev), c.alloc_stream));
   c.device_bytes = records * 2 * sizeof(float4) + coords * sizeof(double) + lut.size() * sizeof(float4) +
-                   cells.size() * sizeof(float4) +
+                   walk.size() * sizeof(float2) +
                    sizeof(CubeDev);
 
   // interior values: one strided 3D copy from the caller's x-fastest array
@@ -177,16 +177,16 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   p.kind = cudaMemcpyHostToDevice;
   CKU(cudaMemcpy3DAsync(&p, st));
   CKU(launch_cube_fill(nullptr, nx, ny, nz, scalar, st));
-  CKU(launch_cube_records(scalar, nx, ny, nz, c.d_vals, st));
-  if (c.alloc_stream) CKU(cudaFreeAsync(scalar, st));
-
   // (the host vectors below stay alive until the synchronize at the end)
   std::vector<double> all;
   all.reserve(coords);
   for (int k = 0; k < 3; ++k) all.insert(all.end(), c.c[k].begin(), c.c[k].end());
   CKU(cudaMemcpyAsync(c.d_c64, all.data(), coords * sizeof(double), cudaMemcpyHostToDevice, st));
+  CKU(launch_cube_records(scalar, nx, ny, nz, c.d_c64, c.d_c64 + nx, c.d_c64 + nx + ny, c.d_vals, st));
+  if (c.alloc_stream) CKU(cudaFreeAsync(scalar, st));
+
   if (!lut.empty()) CKU(cudaMemcpyAsync(c.d_lut, lut.data(), lut.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CKU(cudaMemcpyAsync(c.d_cells, cells.data(), cells.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+  CKU(cudaMemcpyAsync(c.d_cells, walk.data(), walk.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
 
   size_t off = 0;
   for (int k = 0; k < 3; ++k) {
@@ -209,7 +209,10 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   d.cx = (uint32_t)(nx + 1);
   d.cxy = (uint32_t)((nx + 1) * (ny + 1));
   d.lut = c.d_lut;
-  for (int k = 0; k < 3; ++k) d.cells[k] = c.d_cells + cell_off[k];
+  for (int k = 0; k < 3; ++k) {
+    d.walk_up[k] = c.d_cells + up_off[k];
+    d.walk_dn[k] = c.d_cells + dn_off[k];
+  }
   CKU(cudaMemcpyAsync(c.d_desc, &d, sizeof d, cudaMemcpyHostToDevice, st));
   CKU(cudaStreamSynchronize(st));
   if (!c.alloc_stream) CKU(cudaFree(scalar));
@@ -227,7 +230,7 @@ size_t cube_device_bytes(const birp_cube& c) {
   if (!all_uniform)
     for (int k = 0; k < 3; ++k)
       lut += (size_t)std::max(1.0, std::ceil((c.c[k].back() - c.c[k].front()) / c.min_gap[k])) * sizeof(float4);
-  const size_t cells = (coords + 3) * sizeof(float4);
+  const size_t cells = 2 * (coords + 3) * sizeof(float2);
   const size_t records = ((size_t)c.n[0] + 1) * ((size_t)c.n[1] + 1) * ((size_t)c.n[2] + 1);
   return records * 2 * sizeof(float4) + coords * sizeof(double) + lut + cells + sizeof(CubeDev);
 }

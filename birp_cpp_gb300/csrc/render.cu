@@ -439,18 +439,20 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   int nsamp = iters;  // samples this lane evaluates (for the counters)
   if constexpr (KIND == SPACE_CUBE && AXES == AXES_DDA) {
     // Cell-space integration. A lane takes a contiguous run of its ray's
-    // samples and walks the cells the run crosses. Per axis the cell fraction
-    // is affine in the sample index u (fr = fbs + u * fst) and the ray leaves
-    // the cell at u = E (fr reaches 1 moving up, 0 moving down). Within one
-    // cell the trilinear polynomial along the ray is a cubic in u, so the
-    // sum over the m samples in the cell is a0 m + a1 S1 + a2 S2 + a3 S3 with
-    // the power sums S_p = sum_{j<m} j^p and a_p the cubic's coefficients at
-    // the cell's first sample: one 32-byte record and ~30 FMAs per cell
-    // instead of per sample. Sample counts are exact integers and the field
-    // is continuous across cell faces, so a sample on a face may go to either
-    // cell. The walk is confined to cells [-1, n-1] by the sentinel table
-    // entries, so every load is in bounds by construction; the loop is also
-    // capped at (samples + cells + 4) steps.
+    // samples and walks the cells the run crosses. Per axis the sample
+    // position relative to the current cell's base node is affine in the
+    // sample index u (x = xb + u * st) and the ray leaves the cell at
+    // u = ex, where it reaches the cell's exit plane. Within one cell the
+    // trilinear polynomial along the ray is a cubic in u, so the sum over the
+    // m samples in the cell is a0 m + a1 S1 + a2 S2 + a3 S3 with the power
+    // sums S_p = sum_{j<m} j^p and a_p the cubic's coefficients at the
+    // cell's first sample: one 32-byte record and ~30 FMAs per cell instead
+    // of per sample, and one 8-byte walk-table entry per cell face crossed.
+    // Sample counts are exact integers and the field is continuous across
+    // cell faces, so a sample on a face may go to either cell. The walk is
+    // confined to cells [-1, n-1] by the guard cells' infinite exit planes,
+    // so every load is in bounds by construction; the loop is also capped at
+    // (samples + cells + 4) steps.
     const CubeDev& C = *R.cube;
     const int total = b - a;
     const int seglen = (total + S - 1) >> SEGL2;
@@ -458,10 +460,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     const int count = max(0, min(total - seg * seglen, seglen));
     nsamp = count;
     // per axis: position step st, its reciprocal, position at the run's first
-    // sample, the current cell's fraction slope/intercept and exit index, the
-    // direction sg, the exit side tk (1 moving up, 0 down) and the record step
-    float st[3], rst[3], bs[3], fst[3], fbs[3], ex[3], tk[3], sg[3];
-    const float4* cell[3];
+    // sample, the run's first position relative to the current cell's base
+    // node (xb), the exit index ex, the walk-table pointer and the record step
+    float st[3], rst[3], bs[3], xb[3], ex[3];
+    const float2* wt[3];
     int dstr[3];
     const float4* q = C.rec;
     if (count > 0) {
@@ -473,26 +475,26 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         st[k] = R.dt32 * d32[k];
         rst[k] = 1.0f / st[k];  // samples per unit length along the axis (inf if d = 0)
         bs[k] = fmaf(f0, st[k], fmaf(0.5f, st[k], R.pos32[k]));
-        // direction from the sign bit, so that a zero step of either sign
-        // (rst = +-inf) gives an exit index of +inf (or NaN), never a crossing
-        sg[k] = signbit(d32[k]) ? -1.f : 1.f;
-        tk[k] = signbit(d32[k]) ? 0.f : 1.f;
         float idx = A.uniform ? (bs[k] - A.c0) * A.inv_h : lut_index(A, C.lut, bs[k]);
         int kb;
         magic_floor(fminf(fmaxf(idx, 0.f), (float)(A.n - 2)), kb);
         k0s[k] = kb - kMagicBits;
-        cell[k] = C.cells[k] + k0s[k];
-        const float4 e = __ldg(cell[k]);
-        fst[k] = st[k] * e.x;
-        fbs[k] = fmaf(bs[k], e.x, e.y);
-        // exit index of the cell along this axis: (tk - fr(0)) / fst =
-        // (tk - fbs) * w / st (NaN at a sentinel, whose width is inf, and +inf
-        // when the axis is not crossed)
-        ex[k] = (tk[k] - fbs[k]) * (rst[k] * e.z);
+        // direction from the sign bit: a zero step of either sign (rst =
+        // +-inf) then gives an exit index of +inf (or NaN), never a crossing
+        const bool up = !signbit(d32[k]);
+        wt[k] = up ? C.walk_up[k] + k0s[k] : C.walk_dn[k] - k0s[k];
+        const float2 e = __ldg(wt[k]);  // {base node, exit plane}
+        xb[k] = bs[k] - e.x;
+        // exit index of the cell along this axis: bs + ex * st = exit plane
+        ex[k] = (e.y - bs[k]) * rst[k];
         const int stride = (int)record_stride(C.cx, C.cxy, k);
-        dstr[k] = 2 * (sg[k] > 0.f ? stride : -stride);
+        dstr[k] = 2 * (up ? stride : -stride);
       }
       q = C.rec + 2 * record_index(C.cx, C.cxy, k0s[0], k0s[1], k0s[2]);
+      // the ray's step products, the same in every cell (local coordinates
+      // are physical offsets)
+      const float DxDy = st[0] * st[1], DxDz = st[0] * st[2], DyDz = st[1] * st[2];
+      const float DxDyDz = DxDy * st[2];
       const float ub = (float)count;
       float u = 0.f;
       const int cap = count + C.ax[0].n + C.ax[1].n + C.ax[2].n + 4;
@@ -502,8 +504,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         const float nxt = fminf(ceilf(fminf(fminf(ex[0], ex[1]), ex[2])), ub);
         if (nxt > u) {
           const float m = nxt - u;
-          const float X = fmaf(u, fst[0], fbs[0]), Y = fmaf(u, fst[1], fbs[1]), Z = fmaf(u, fst[2], fbs[2]);
-          const float Dx = fst[0], Dy = fst[1], Dz = fst[2];
+          const float X = fmaf(u, st[0], xb[0]), Y = fmaf(u, st[1], xb[1]), Z = fmaf(u, st[2], xb[2]);
           // value, gradient and mixed second derivatives at the first sample
           const float b0 = fmaf(lo.y, X, lo.x);  // c0 + c1 X
           const float a0 = fmaf(lo.w, X, lo.z);  // c2 + c4 X
@@ -514,10 +515,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           const float gy = fmaf(a1, Z, a0);
           const float hxy = fmaf(hi.w, Z, lo.w), hxz = fmaf(hi.w, Y, hi.y);  // c4 + c7 Z, c5 + c7 Y
           const float gx = fmaf(hxz, Z, fmaf(lo.w, Y, lo.y));  // c1 + c4 Y + c5 Z + c7 Y Z
-          const float p1 = fmaf(gx, Dx, fmaf(gy, Dy, gz * Dz));
-          const float DxDy = Dx * Dy;
-          const float p2 = fmaf(hxy, DxDy, fmaf(hxz, Dx * Dz, a1 * (Dy * Dz)));
-          const float p3 = hi.w * (DxDy * Dz);
+          const float p1 = fmaf(gx, st[0], fmaf(gy, st[1], gz * st[2]));
+          const float p2 = fmaf(hxy, DxDy, fmaf(hxz, DxDz, a1 * DyDz));
+          const float p3 = hi.w * DxDyDz;
           const float mm1 = m * (m - 1.f);
           const float s1 = 0.5f * mm1;
           const float s2 = mm1 * (2.f * m - 1.f) * (1.f / 6.f);
@@ -526,16 +526,15 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           u = nxt;
           ++ncell;
         }
-        // step every axis whose exit index has been reached; the sentinel's
-        // exit index is NaN, which ends the loop at the table's end
+        // step every axis whose exit index has been reached; a guard cell's
+        // exit index is +inf, which ends the walk at the table's end
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
           while (ex[k] <= u) {
-            cell[k] += (sg[k] > 0.f ? 1 : -1);
-            const float4 en = __ldg(cell[k]);
-            fst[k] = st[k] * en.x;
-            fbs[k] = fmaf(bs[k], en.x, en.y);
-            ex[k] = (tk[k] - fbs[k]) * (rst[k] * en.z);
+            ++wt[k];
+            const float2 e = __ldg(wt[k]);
+            xb[k] = bs[k] - e.x;
+            ex[k] = (e.y - bs[k]) * rst[k];
             q += dstr[k];
           }
         }
@@ -754,8 +753,16 @@ __global__ void cube_guard_kernel(float* dst, int nx, int ny, int nz) {
 // Cell records from the padded scalar grid ((nx+2)(ny+2)(nz+2), node i at
 // padded index i+1): record (a, b, c), a in [0, nx], is the trilinear
 // polynomial of the 8 padded nodes (a..a+1, b..b+1, c..c+1) (cell a-1 of the
-// unpadded grid), coefficients computed in FP64 and rounded once.
-__global__ void cube_records_kernel(const float* __restrict__ v, int nx, int ny, int nz, float4* __restrict__ rec) {
+// unpadded grid) in local physical coordinates: the fraction coefficients
+// times the inverse cell widths (0 for a guard cell, whose two faces along
+// that axis hold equal values), computed in FP64 and rounded once.
+__device__ __forceinline__ double inv_width(const double* c, int n, long long a) {
+  return (a >= 1 && a <= n - 1) ? 1.0 / (c[a] - c[a - 1]) : 0.0;
+}
+
+__global__ void cube_records_kernel(const float* __restrict__ v, int nx, int ny, int nz, const double* __restrict__ cx64,
+                                    const double* __restrict__ cy64, const double* __restrict__ cz64,
+                                    float4* __restrict__ rec) {
   const long long cx = nx + 1, cy = ny + 1, cz = nz + 1, px = nx + 2, pxy = (long long)(nx + 2) * (ny + 2);
   const long long n = cx * cy * cz;
   for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
@@ -763,11 +770,12 @@ __global__ void cube_records_kernel(const float* __restrict__ v, int nx, int ny,
     const float* p = v + c * pxy + b * px + a;
     const double v000 = p[0], v001 = p[1], v010 = p[px], v011 = p[px + 1];
     const double v100 = p[pxy], v101 = p[pxy + 1], v110 = p[pxy + px], v111 = p[pxy + px + 1];
-    const double c1 = v001 - v000, c2 = v010 - v000, c3 = v100 - v000;
-    const double c4 = (v011 - v010) - (v001 - v000);
-    const double c5 = (v101 - v100) - (v001 - v000);
-    const double c6 = (v110 - v100) - (v010 - v000);
-    const double c7 = ((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000));
+    const double ix = inv_width(cx64, nx, a), iy = inv_width(cy64, ny, b), iz = inv_width(cz64, nz, c);
+    const double c1 = (v001 - v000) * ix, c2 = (v010 - v000) * iy, c3 = (v100 - v000) * iz;
+    const double c4 = ((v011 - v010) - (v001 - v000)) * (ix * iy);
+    const double c5 = ((v101 - v100) - (v001 - v000)) * (ix * iz);
+    const double c6 = ((v110 - v100) - (v010 - v000)) * (iy * iz);
+    const double c7 = (((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000))) * (ix * iy * iz);
     rec[2 * r] = make_float4((float)v000, (float)c1, (float)c2, (float)c4);
     rec[2 * r + 1] = make_float4((float)c3, (float)c5, (float)c6, (float)c7);
   }
@@ -796,7 +804,7 @@ __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int triline
         else hi = mid;
       }
       k[a] = lo;
-      f[a] = (p[a] - A.c64[lo]) / (A.c64[lo + 1] - A.c64[lo]);
+      f[a] = p[a] - A.c64[lo];  // local coordinate in the cell
     }
     if (!in) {
       out[t] = -1.f;
@@ -937,10 +945,11 @@ cudaError_t launch_cube_fill(const float*, int nx, int ny, int nz, float* dst, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, float4* rec, cudaStream_t s) {
+cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, const double* cx64, const double* cy64,
+                                const double* cz64, float4* rec, cudaStream_t s) {
   const long long n = (long long)(nx + 1) * (ny + 1) * (nz + 1);
   int blocks = (int)std::min<long long>((n + 255) / 256, 8192);
-  cube_records_kernel<<<blocks, 256, 0, s>>>(padded, nx, ny, nz, rec);
+  cube_records_kernel<<<blocks, 256, 0, s>>>(padded, nx, ny, nz, cx64, cy64, cz64, rec);
   return cudaGetLastError();
 }
 
