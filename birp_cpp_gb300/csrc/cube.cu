@@ -141,7 +141,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   // cells take the edge node as base (their coefficients along the axis are
   // 0) and an infinite exit plane, so the walk stops there.
   std::vector<float2> walk;
-  walk.reserve(2 * (coords + 3));
+  walk.reserve(2 * (coords + 3) + 1);
   size_t up_off[3], dn_off[3];
   for (int k = 0; k < 3; ++k) {
     const std::vector<double>& ck = c.c[k];
@@ -155,6 +155,9 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     dn_off[k] = walk.size() - 1;  // cell 0
     walk.push_back(make_float2((float)ck[0], -INFINITY));  // cell -1
   }
+  // one padding entry: a walk that reads one entry ahead of its cell may
+  // read one past the last table's guard cell (the value is never used)
+  walk.push_back(make_float2(0.f, 0.f));
   CKU(dev_alloc(&c.d_cells, walk.size() * sizeof(float2), c.alloc_stream));
   const size_t records = ((size_t)nx + 1) * ((size_t)ny + 1) * ((size_t)nz + 1);
   CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
@@ -230,7 +233,7 @@ size_t cube_device_bytes(const birp_cube& c) {
   if (!all_uniform)
     for (int k = 0; k < 3; ++k)
       lut += (size_t)std::max(1.0, std::ceil((c.c[k].back() - c.c[k].front()) / c.min_gap[k])) * sizeof(float4);
-  const size_t cells = 2 * (coords + 3) * sizeof(float2);
+  const size_t cells = (2 * (coords + 3) + 1) * sizeof(float2);
   const size_t records = ((size_t)c.n[0] + 1) * ((size_t)c.n[1] + 1) * ((size_t)c.n[2] + 1);
   return records * 2 * sizeof(float4) + coords * sizeof(double) + lut + cells + sizeof(CubeDev);
 }

@@ -378,6 +378,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 
   const int N = R.N;
   int a = 0, b = N;
+  // per-lane telemetry, summed over the warp at the end (one atomic per warp)
+  unsigned int n_exact = 0, n_cells = 0;
   if constexpr (KIND == SPACE_CUBE) {
     const CubeDev& C = *R.cube;
     AxisEst est[3];
@@ -403,7 +405,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     if (!certain && valid) {
       need_d64();
       int s = 0, e = N;
-#pragma unroll 1
+#pragma unroll
       for (int k = 0; k < 3; ++k) {
         int sk, ek;
         if (est[k].parallel || est[k].s_lo != est[k].s_hi || est[k].e_lo != est[k].e_hi) {
@@ -424,7 +426,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         a = s;
         b = e;
       }
-      if (stats) atomicAdd(&stats->exact_range_rays, 1ull);
+      n_exact = (threadIdx.x & ((1 << R.seg_log2) - 1)) == 0;  // once per ray
     }
     if (b < a) b = a;
   }
@@ -539,7 +541,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           }
         }
       }
-      if (stats) atomicAdd(&stats->cells, (unsigned long long)ncell);
+      n_cells = (unsigned int)ncell;
     }
   } else if constexpr (KIND == SPACE_CUBE) {
     // nearest by truncation (UNIFORM / LUT index)
@@ -646,6 +648,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   if (stats) {
     unsigned int cnt = __reduce_add_sync(0xffffffffu, (unsigned int)nsamp);
     if (lane == 0 && cnt) atomicAdd(&stats->samples, (unsigned long long)cnt);
+    const unsigned int ce = __reduce_add_sync(0xffffffffu, n_exact);
+    const unsigned int cc = __reduce_add_sync(0xffffffffu, n_cells);
+    if (lane == 0 && ce) atomicAdd(&stats->exact_range_rays, (unsigned long long)ce);
+    if (lane == 0 && cc) atomicAdd(&stats->cells, (unsigned long long)cc);
   }
   // merge the S partial sums of a ray
   float hi = acc.s, lo = -acc.c;
