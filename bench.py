@@ -416,14 +416,25 @@ def main():
     import ctypes as C
     arr = B.Batch._reqs(items)
     ptrs = (C.c_void_p * len(items))(*[o.ctypes.data for o in outs])
+    # untimed calls with the same output buffers (their pages are then mapped,
+    # as in a serving loop that reuses its buffers)
+    for _ in range(max(args.warmup, 1)):
+        B.check(B.lib().birp_batch_render(batch.h, arr, len(items), ptrs))
+    e2e_dev = []
     for _ in range(args.steps):
         B.flush_l2()
         barrier(world)
         t0 = time.perf_counter()
         B.check(B.lib().birp_batch_render(batch.h, arr, len(items), ptrs))
         e2e_t.append(time.perf_counter() - t0)
+        e2e_dev.append(batch.last_ms())
     e2e_s = allreduce_max(world, float(np.mean(e2e_t)))
     e2e = world * args.requests / e2e_s
+    # where the end-to-end time goes: kernel, device->host copy, host side
+    k_mean = float(np.mean([k for k, _ in e2e_dev]))
+    t_mean = float(np.mean([t for _, t in e2e_dev]))
+    e2e_breakdown = {"kernel_ms": k_mean, "d2h_ms": t_mean - k_mean,
+                     "host_ms": float(np.mean(e2e_t)) * 1e3 - t_mean}
 
     # ---- parity spot check of the timed images against the FP64 oracle
     parity = spot_check(W, outs) if rank == 0 else None
@@ -522,6 +533,7 @@ def main():
             "batched_vs_plain": (value / plain) if plain else None,
             "by_size": by_size,
             "e2e_vs_plain": (e2e / plain) if plain else None,
+            "e2e_breakdown": e2e_breakdown,
             "serving": serving,
             "ray_samples_per_s": samples_per_step * world / (step_ms / 1000.0),
             "roofline": roofline, "roofline_per_sample": roofline_per_sample, "roofline_hbm": roofline_hbm,

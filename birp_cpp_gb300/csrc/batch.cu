@@ -95,7 +95,7 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   return ok();
 }
 
-birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n) {
+birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* const* direct_outs) {
   if (birp_status s = check_init()) return s;
   if (!b || n < 0 || (n > 0 && !reqs)) return fail(BIRP_ERR_INVALID, "bad argument");
   if (n > b->max_req) return fail(BIRP_ERR_INVALID, "%d requests exceed the batch limit %d", n, b->max_req);
@@ -118,7 +118,8 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n) {
       return fail(BIRP_ERR_INVALID, "batch images need more than %lld pixels", (long long)b->max_px);
     b->offsets[i] = used;
     b->npx[i] = npx;
-    if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, b->d_out + used, rq[i])) return s;
+    float* out = direct_outs ? direct_outs[i] : b->d_out + used;
+    if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, out, rq[i])) return s;
     used += npx;
     work[i] = (double)npx * c.n_samples * (reqs[i].cmem ? 16.0 : 1.0);
     if (reqs[i].cmem || !c.trilinear) cls = BATCH_ANY;
@@ -132,12 +133,14 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n) {
   hdr[1] = first[n];
   b->n = n;
   b->used = used;
+  b->direct = direct_outs != nullptr;
   cudaError_t e;
   if ((e = cudaEventRecord(b->e_start, b->stream)) != cudaSuccess ||
       (e = cudaGraphLaunch(b->exec[cls], b->stream)) != cudaSuccess ||
       (e = cudaEventRecord(b->e_kernel, b->stream)) != cudaSuccess ||
-      (used > 0 && (e = cudaMemcpyAsync(b->h_out, b->d_out, (size_t)used * sizeof(float), cudaMemcpyDeviceToHost,
-                                        b->stream)) != cudaSuccess) ||
+      (used > 0 && !b->direct &&
+       (e = cudaMemcpyAsync(b->h_out, b->d_out, (size_t)used * sizeof(float), cudaMemcpyDeviceToHost,
+                            b->stream)) != cudaSuccess) ||
       (e = cudaEventRecord(b->e_end, b->stream)) != cudaSuccess)
     return fail(BIRP_ERR_CUDA, "batch launch: %s", cudaGetErrorString(e));
   b->pending = true;
@@ -171,16 +174,28 @@ birp_status birp_batch_submit(birp_batch* b, const birp_request* reqs, int n) { 
 birp_status birp_batch_wait(birp_batch* b) { return batch_wait(b); }
 
 const float* birp_batch_image(const birp_batch* b, int i) {
-  if (!b || i < 0 || i >= b->n || b->pending) return nullptr;
+  if (!b || i < 0 || i >= b->n || b->pending || b->direct) return nullptr;
   return b->h_out + b->offsets[i];
 }
 
 birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, float* const* outs) {
   if (n > 0 && !outs) return fail(BIRP_ERR_INVALID, "outs is NULL");
+  bool direct = host_direct_writes() && n > 0;
+  for (int i = 0; i < n && direct; ++i) direct = outs[i] != nullptr;
+  if (direct) {
+    // the kernel writes each image straight into the caller's buffer
+    if (birp_status s = batch_submit(b, reqs, n, outs)) return s;
+    return batch_wait(b);
+  }
   if (birp_status s = batch_submit(b, reqs, n)) return s;
   if (birp_status s = batch_wait(b)) return s;
-  for (int i = 0; i < n; ++i)
-    if (outs[i]) std::memcpy(outs[i], b->h_out + b->offsets[i], (size_t)b->npx[i] * sizeof(float));
+  std::vector<const float*> src(n);
+  std::vector<size_t> cnt(n);
+  for (int i = 0; i < n; ++i) {
+    src[i] = b->h_out + b->offsets[i];
+    cnt[i] = (size_t)b->npx[i];
+  }
+  parallel_copy(outs, src.data(), cnt.data(), n);
   return ok();
 }
 

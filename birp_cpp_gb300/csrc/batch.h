@@ -19,6 +19,7 @@ struct birp_batch {
   int64_t used = 0;
   int grid[2] = {0, 0};
   bool pending = false;
+  bool direct = false;       // the last launch wrote the caller's host images itself
   cudaStream_t stream = nullptr;
   // one graph per persistent-kernel class (birp::BatchClass)
   cudaGraph_t graph[2] = {nullptr, nullptr};
@@ -28,6 +29,8 @@ struct birp_batch {
 
 namespace birp {
 birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out);
-birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n);
+// direct_outs: when given, request i's image is written by the kernel into
+// direct_outs[i] (host memory the device can write) and nothing is copied back
+birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* const* direct_outs = nullptr);
 birp_status batch_wait(birp_batch* b);
 }  // namespace birp

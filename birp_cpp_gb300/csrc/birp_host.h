@@ -44,9 +44,17 @@ struct Context {
   float* xyz_scratch = nullptr;  // point-sample buffers
   size_t xyz_floats = 0;
   void* flush = nullptr;         // L2 flush buffer (timing)
+  int pageable_access = 0;       // kernels may write pageable host memory
   std::mutex mu;
 };
 extern Context g_ctx;
+
+// True when render outputs in host memory are written by the kernels
+// directly (the device reads and writes pageable host memory coherently,
+// e.g. over NVLink-C2C); BIRP_HOST_DIRECT=0 in the environment turns it off.
+bool host_direct_writes();
+// memcpy of many (dst, src, bytes) pieces on up to 8 host threads.
+void parallel_copy(float* const* dst, const float* const* src, const size_t* floats, int n);
 
 // FP64 camera frame (see camera_frame in capi.cu).
 struct Frame {

@@ -5,10 +5,12 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/birp_gb300.h"
@@ -250,6 +252,34 @@ birp_status check_init() {
 
 cudaStream_t pick_stream(void* s) { return s ? (cudaStream_t)s : g_ctx.stream; }
 
+bool host_direct_writes() {
+  if (!g_ctx.pageable_access) return false;
+  const char* v = std::getenv("BIRP_HOST_DIRECT");
+  return !(v && v[0] == '0');
+}
+
+void parallel_copy(float* const* dst, const float* const* src, const size_t* floats, int n) {
+  size_t total = 0;
+  for (int i = 0; i < n; ++i) total += dst[i] ? floats[i] : 0;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = (int)std::min<size_t>({8, hw, total / (1u << 20) + 1});  // >= 4 MB per thread
+  // thread t copies the floats [t * total / nt, (t + 1) * total / nt) of the concatenation
+  auto work = [&](int t) {
+    const size_t lo = total * t / nt, hi = total * (t + 1) / nt;
+    size_t base = 0;
+    for (int i = 0; i < n && base < hi; ++i) {
+      if (!dst[i]) continue;
+      const size_t a = std::max(lo, base), b = std::min(hi, base + floats[i]);
+      if (a < b) std::memcpy(dst[i] + (a - base), src[i] + (a - base), (b - a) * sizeof(float));
+      base += floats[i];
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
+}
+
 }  // namespace birp
 
 #define CK(x)                                                                                  \
@@ -280,6 +310,7 @@ birp_status birp_init(int device) {
   CK(cudaMalloc(&g_ctx.stats, sizeof(KernelStats)));
   CK(cudaMemset(g_ctx.stats, 0, sizeof(KernelStats)));
   CK(cudaDeviceGetAttribute(&g_ctx.sms, cudaDevAttrMultiProcessorCount, device));
+  CK(cudaDeviceGetAttribute(&g_ctx.pageable_access, cudaDevAttrPageableMemoryAccess, device));
   g_ctx.device = device;
   return ok();
 }
@@ -503,12 +534,18 @@ birp_status birp_render(const birp_cube* cube, const birp_cmem* cmem, const birp
   if (birp_status s = validate_camera(cam)) return s;
   std::lock_guard<std::mutex> lk(g_ctx.mu);
   const size_t npx = (size_t)cam->nx * cam->ny;
-  if (birp_status s = ensure_scratch(npx)) return s;
-  RequestDev r;
-  if (birp_status s = build_request(cube, cmem, *cam, g_ctx.scratch, r)) return s;
   cudaStream_t st = pick_stream(stream);
-  CK(launch_render_plain(r, g_ctx.stats, st));
-  CK(cudaMemcpyAsync(out_host, g_ctx.scratch, npx * sizeof(float), cudaMemcpyDeviceToHost, st));
+  RequestDev r;
+  if (host_direct_writes()) {
+    // the kernel writes every pixel of the caller's image itself
+    if (birp_status s = build_request(cube, cmem, *cam, out_host, r)) return s;
+    CK(launch_render_plain(r, g_ctx.stats, st));
+  } else {
+    if (birp_status s = ensure_scratch(npx)) return s;
+    if (birp_status s = build_request(cube, cmem, *cam, g_ctx.scratch, r)) return s;
+    CK(launch_render_plain(r, g_ctx.stats, st));
+    CK(cudaMemcpyAsync(out_host, g_ctx.scratch, npx * sizeof(float), cudaMemcpyDeviceToHost, st));
+  }
   CK(cudaStreamSynchronize(st));
   return ok();
 }

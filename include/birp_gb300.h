@@ -128,7 +128,11 @@ void birp_camera_defaults(birp_camera* cam);
 /* Renders one image of a cube (cmem == NULL) or of CMEM (cube == NULL) into a
  * HOST array of ny*nx floats; returns when the image is in out_host.
  * Replaces Camera::Render (src/Camera.cpp:63-233) — except that the output is
- * overwritten, where the reference adds to Camera::image. */
+ * overwritten, where the reference adds to Camera::image. Where the device
+ * accesses pageable host memory coherently (cudaDevAttrPageableMemoryAccess,
+ * e.g. Grace over NVLink-C2C) the kernel writes out_host itself; otherwise
+ * the image is copied back. BIRP_HOST_DIRECT=0 in the environment forces the
+ * copy. */
 birp_status birp_render(const birp_cube* cube, const birp_cmem* cmem, const birp_camera* cam, float* out_host,
                         void* stream);
 /* Same, into DEVICE memory, asynchronous on the stream. */
@@ -165,9 +169,13 @@ birp_status birp_batch_submit(birp_batch* b, const birp_request* reqs, int n);
  * buffer (birp_batch_image). */
 birp_status birp_batch_wait(birp_batch* b);
 /* Pointer to request i's image in the pinned host buffer, valid until the
- * next submit. */
+ * next submit (NULL after a birp_batch_render that wrote the caller's
+ * buffers directly). */
 const float* birp_batch_image(const birp_batch* b, int i);
-/* submit + wait + copy each image to outs[i] (host arrays of ny*nx floats). */
+/* submit + wait, with each image in outs[i] (host arrays of ny*nx floats):
+ * written by the kernel itself where the device accesses pageable host
+ * memory (as birp_render), else copied from the pinned buffer on several
+ * host threads. */
 birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, float* const* outs);
 /* Renders n requests (n <= 256) like birp_batch_submit but allocates nothing,
  * for callers that cannot call cudaMalloc on their render path (code running

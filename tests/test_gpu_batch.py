@@ -63,6 +63,32 @@ def test_batch_single_and_empty(birp, spaces):
     b.close()
 
 
+def test_host_outputs_direct_and_copied(birp, spaces, monkeypatch):
+    """birp_batch_render and birp_render give the same bits whether the kernel
+    writes the caller's host buffers itself (devices with coherent pageable
+    host access) or the images are copied back (BIRP_HOST_DIRECT=0), and the
+    same as the pinned-buffer path of submit / wait."""
+    import ctypes as C
+    items = mixed_items(birp, spaces, n=20, seed=21)
+    b = birp.Batch(64, 1 << 22)
+    direct = b.render(items)
+    monkeypatch.setenv("BIRP_HOST_DIRECT", "0")
+    copied = b.render(items)
+    plain_copied = [birp.render(sp, cam) for sp, cam in items]
+    monkeypatch.delenv("BIRP_HOST_DIRECT")
+    plain_direct = [birp.render(sp, cam) for sp, cam in items]
+    b.submit(items)
+    b.wait()
+    lib = birp.lib()
+    lib.birp_batch_image.restype = C.POINTER(C.c_float)
+    for i, (sp, cam) in enumerate(items):
+        p = lib.birp_batch_image(b.h, i)
+        pinned = np.ctypeslib.as_array(p, shape=(cam.ny, cam.nx)).copy()
+        for other in (copied[i], plain_copied[i], plain_direct[i], pinned):
+            assert np.array_equal(direct[i], other)
+    b.close()
+
+
 def test_server_same_alone_and_in_mix(birp, spaces):
     """Each request's image from the server equals its plain render, whether
     it ran alone or mixed with others arriving concurrently."""
