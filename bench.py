@@ -538,7 +538,9 @@ def main():
             "ray_samples_per_s": samples_per_step * world / (step_ms / 1000.0),
             "roofline": roofline, "roofline_per_sample": roofline_per_sample, "roofline_hbm": roofline_hbm,
             "cpu_baseline": cpu, "parity": parity,
-            "gpu_launches": args.steps, "clocks": clocks.summary(),
+            # each step replays one graph with two kernels: the general one
+            # (no work here) and the trilinear-cube one
+            "gpu_launches": 2 * args.steps, "clocks": clocks.summary(),
             "exact_fp64_rays_per_step": ks["exact_range_rays"] / args.steps,
             "samples_per_cell": (ks["samples"] / ks["cells"]) if ks.get("cells") else None,
         }

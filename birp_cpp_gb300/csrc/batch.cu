@@ -4,7 +4,6 @@
 // (src/main.cpp:242-264).
 #include <algorithm>
 #include <cstring>
-#include <numeric>
 #include <vector>
 
 #include "batch.h"
@@ -26,10 +25,8 @@ static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 static void free_batch(birp_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
-  for (int c = 0; c < 2; ++c) {
-    if (b->exec[c]) cudaGraphExecDestroy(b->exec[c]);
-    if (b->graph[c]) cudaGraphDestroy(b->graph[c]);
-  }
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
   if (b->h_stage) cudaFreeHost(b->h_stage);
   if (b->h_out) cudaFreeHost(b->h_out);
   if (b->d_stage) cudaFree(b->d_stage);
@@ -49,10 +46,17 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   birp_batch* b = new birp_batch();
   b->max_req = max_requests;
   b->max_px = max_pixels;
-  // staging block: hdr[4] | first[max+1] | order[max] | (16B aligned) RequestDev[max]
-  b->off_first = 4 * sizeof(int);
-  b->off_order = b->off_first + (size_t)(max_requests + 1) * sizeof(int);
-  b->off_reqs = align_up(b->off_order + (size_t)max_requests * sizeof(int), 16);
+  // staging block: hdr[2][4] | first[2][max+1] | order[2][max] | (16B aligned) RequestDev[max]
+  size_t off = 8 * sizeof(int);
+  for (int c = 0; c < 2; ++c) {
+    b->off_first[c] = off;
+    off += (size_t)(max_requests + 1) * sizeof(int);
+  }
+  for (int c = 0; c < 2; ++c) {
+    b->off_order[c] = off;
+    off += (size_t)max_requests * sizeof(int);
+  }
+  b->off_reqs = align_up(off, 16);
   b->stage_bytes = b->off_reqs + (size_t)max_requests * sizeof(RequestDev);
   auto bail = [&](birp_status s) {
     free_batch(b);
@@ -62,7 +66,7 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaHostAlloc(&b->h_stage, b->stage_bytes, cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaMalloc(&b->d_stage, b->stage_bytes)) != cudaSuccess ||
-      (e = cudaMalloc(&b->d_counter, sizeof(unsigned int))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_counter, 2 * sizeof(unsigned int))) != cudaSuccess ||
       (e = cudaMalloc(&b->d_out, (size_t)max_pixels * sizeof(float))) != cudaSuccess ||
       (e = cudaHostAlloc(&b->h_out, (size_t)max_pixels * sizeof(float), cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaEventCreate(&b->e_start)) != cudaSuccess || (e = cudaEventCreate(&b->e_kernel)) != cudaSuccess ||
@@ -71,26 +75,30 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
                      cudaGetErrorString(e)));
   std::memset(b->h_stage, 0, b->stage_bytes);
 
-  BatchDev bd;
-  bd.hdr = reinterpret_cast<const int*>(b->d_stage);
-  bd.first = reinterpret_cast<const int*>(b->d_stage + b->off_first);
-  bd.order = reinterpret_cast<const int*>(b->d_stage + b->off_order);
-  bd.reqs = reinterpret_cast<const RequestDev*>(b->d_stage + b->off_reqs);
-  bd.counter = b->d_counter;
-  bd.stats = g_ctx.stats;
-  // capture per kernel class: descriptors H2D, queue head reset, persistent kernel
-  for (int cls = 0; cls < 2; ++cls) {
-    b->grid[cls] = persistent_grid(cls);
-    if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-      return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
-    cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
-    cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), b->stream);
-    launch_render_batch(bd, b->grid[cls], b->stream, cls);
-    e = cudaStreamEndCapture(b->stream, &b->graph[cls]);
-    if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
-    if ((e = cudaGraphInstantiate(&b->exec[cls], b->graph[cls], 0)) != cudaSuccess)
-      return bail(fail(BIRP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  // One graph: descriptors H2D, both queue heads reset, then the general
+  // kernel (CMEM and nearest requests: few but heavy, so they start first)
+  // and the trilinear-cube kernel (64 registers, full occupancy). A class
+  // with no requests costs one launch whose CTAs exit at once.
+  BatchDev bd[2];
+  for (int c = 0; c < 2; ++c) {
+    bd[c].hdr = reinterpret_cast<const int*>(b->d_stage) + 4 * c;
+    bd[c].first = reinterpret_cast<const int*>(b->d_stage + b->off_first[c]);
+    bd[c].order = reinterpret_cast<const int*>(b->d_stage + b->off_order[c]);
+    bd[c].reqs = reinterpret_cast<const RequestDev*>(b->d_stage + b->off_reqs);
+    bd[c].counter = b->d_counter + c;
+    bd[c].stats = g_ctx.stats;
+    b->grid[c] = persistent_grid(c);
   }
+  if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+  cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
+  cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(unsigned int), b->stream);
+  launch_render_batch(bd[BATCH_ANY], b->grid[BATCH_ANY], b->stream, BATCH_ANY);
+  launch_render_batch(bd[BATCH_CUBE_TRI], b->grid[BATCH_CUBE_TRI], b->stream, BATCH_CUBE_TRI);
+  e = cudaStreamEndCapture(b->stream, &b->graph);
+  if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
+  if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess)
+    return bail(fail(BIRP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)));
   *out = b;
   return ok();
 }
@@ -102,14 +110,12 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* 
   if (b->pending)
     if (birp_status s = batch_wait(b)) return s;
   int* hdr = reinterpret_cast<int*>(b->h_stage);
-  int* first = reinterpret_cast<int*>(b->h_stage + b->off_first);
-  int* order = reinterpret_cast<int*>(b->h_stage + b->off_order);
   RequestDev* rq = reinterpret_cast<RequestDev*>(b->h_stage + b->off_reqs);
   b->offsets.assign(n, 0);
   b->npx.assign(n, 0);
   int64_t used = 0;
   std::vector<double> work(n);
-  int cls = BATCH_CUBE_TRI;
+  std::vector<int> members[2];
   for (int i = 0; i < n; ++i) {
     const birp_camera& c = reqs[i].cam;
     if (birp_status s = validate_camera(&c)) return s;
@@ -122,21 +128,34 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* 
     if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, out, rq[i])) return s;
     used += npx;
     work[i] = (double)npx * c.n_samples * (reqs[i].cmem ? 16.0 : 1.0);
-    if (reqs[i].cmem || !c.trilinear) cls = BATCH_ANY;
+    members[(reqs[i].cmem || !c.trilinear) ? BATCH_ANY : BATCH_CUBE_TRI].push_back(i);
   }
-  // largest work first, so long renders start early and small ones fill the tail
-  std::iota(order, order + n, 0);
-  std::stable_sort(order, order + n, [&](int x, int y) { return work[x] > work[y]; });
-  first[0] = 0;
-  for (int k = 0; k < n; ++k) first[k + 1] = first[k] + rq[order[k]].tiles;
-  hdr[0] = n;
-  hdr[1] = first[n];
+  // per class: largest work first, so long renders start early and small
+  // ones fill the tail
+  for (int cls = 0; cls < 2; ++cls) {
+    int* first = reinterpret_cast<int*>(b->h_stage + b->off_first[cls]);
+    int* order = reinterpret_cast<int*>(b->h_stage + b->off_order[cls]);
+    std::vector<int>& m = members[cls];
+    std::stable_sort(m.begin(), m.end(), [&](int x, int y) { return work[x] > work[y]; });
+    const int k = (int)m.size();
+    first[0] = 0;
+    for (int j = 0; j < k; ++j) {
+      order[j] = m[j];
+      first[j + 1] = first[j] + rq[m[j]].tiles;
+    }
+    hdr[4 * cls] = k;
+    hdr[4 * cls + 1] = first[k];
+  }
   b->n = n;
   b->used = used;
   b->direct = direct_outs != nullptr;
+  if (b->direct) {
+    std::vector<size_t> cnt(b->npx.begin(), b->npx.end());
+    prefault_outputs(direct_outs, cnt.data(), n);
+  }
   cudaError_t e;
   if ((e = cudaEventRecord(b->e_start, b->stream)) != cudaSuccess ||
-      (e = cudaGraphLaunch(b->exec[cls], b->stream)) != cudaSuccess ||
+      (e = cudaGraphLaunch(b->exec, b->stream)) != cudaSuccess ||
       (e = cudaEventRecord(b->e_kernel, b->stream)) != cudaSuccess ||
       (used > 0 && !b->direct &&
        (e = cudaMemcpyAsync(b->h_out, b->d_out, (size_t)used * sizeof(float), cudaMemcpyDeviceToHost,

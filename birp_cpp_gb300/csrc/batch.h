@@ -7,10 +7,12 @@
 struct birp_batch {
   int max_req = 0;
   int64_t max_px = 0;
-  size_t off_first = 0, off_order = 0, off_reqs = 0, stage_bytes = 0;
+  // staging block: hdr[2][4] | first[2][max+1] | order[2][max] | (16 B aligned)
+  // RequestDev[max]; class c's tables describe its share of the requests
+  size_t off_first[2] = {0, 0}, off_order[2] = {0, 0}, off_reqs = 0, stage_bytes = 0;
   char* h_stage = nullptr;   // pinned descriptors of the next launch
   char* d_stage = nullptr;
-  unsigned int* d_counter = nullptr;
+  unsigned int* d_counter = nullptr;  // work queue heads, one per kernel class
   float* d_out = nullptr;    // images of the launch, concatenated
   float* h_out = nullptr;    // pinned copy of the images
   std::vector<int64_t> offsets;
@@ -21,9 +23,9 @@ struct birp_batch {
   bool pending = false;
   bool direct = false;       // the last launch wrote the caller's host images itself
   cudaStream_t stream = nullptr;
-  // one graph per persistent-kernel class (birp::BatchClass)
-  cudaGraph_t graph[2] = {nullptr, nullptr};
-  cudaGraphExec_t exec[2] = {nullptr, nullptr};
+  // {descriptors H2D, queue heads reset, general kernel, trilinear kernel}
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
   cudaEvent_t e_start = nullptr, e_kernel = nullptr, e_end = nullptr;
 };
 

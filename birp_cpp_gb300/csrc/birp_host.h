@@ -55,6 +55,11 @@ extern Context g_ctx;
 bool host_direct_writes();
 // memcpy of many (dst, src, bytes) pieces on up to 8 host threads.
 void parallel_copy(float* const* dst, const float* const* src, const size_t* floats, int n);
+// Writes one float per host page of each output image (on up to 8 threads)
+// so the pages are mapped before a kernel writes them: a device fault on an
+// unmapped page of pageable memory is far slower than a host write. Only for
+// outputs the kernel then overwrites whole.
+void prefault_outputs(float* const* dst, const size_t* floats, int n);
 
 // FP64 camera frame (see camera_frame in capi.cu).
 struct Frame {

@@ -13,6 +13,8 @@
 #include <thread>
 #include <vector>
 
+#include <unistd.h>
+
 #include "../../include/birp_gb300.h"
 #include "birp_host.h"
 #include "birp_internal.h"
@@ -256,6 +258,29 @@ bool host_direct_writes() {
   if (!g_ctx.pageable_access) return false;
   const char* v = std::getenv("BIRP_HOST_DIRECT");
   return !(v && v[0] == '0');
+}
+
+void prefault_outputs(float* const* dst, const size_t* floats, int n) {
+  static const size_t page = [] {
+    long p = sysconf(_SC_PAGESIZE);
+    return (size_t)(p > 0 ? p : 4096) / sizeof(float);
+  }();
+  size_t total = 0;
+  for (int i = 0; i < n; ++i) total += dst[i] ? floats[i] : 0;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const int nt = (int)std::min<size_t>({8, hw, total / (1u << 22) + 1});  // >= 16 MB per thread
+  auto work = [&](int t) {
+    for (int i = t; i < n; i += nt) {
+      if (!dst[i] || !floats[i]) continue;
+      volatile float* p = dst[i];
+      for (size_t k = 0; k < floats[i]; k += page) p[k] = 0.f;
+      p[floats[i] - 1] = 0.f;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+  work(0);
+  for (auto& x : th) x.join();
 }
 
 void parallel_copy(float* const* dst, const float* const* src, const size_t* floats, int n) {
@@ -539,6 +564,7 @@ birp_status birp_render(const birp_cube* cube, const birp_cmem* cmem, const birp
   if (host_direct_writes()) {
     // the kernel writes every pixel of the caller's image itself
     if (birp_status s = build_request(cube, cmem, *cam, out_host, r)) return s;
+    prefault_outputs(&out_host, &npx, 1);
     CK(launch_render_plain(r, g_ctx.stats, st));
   } else {
     if (birp_status s = ensure_scratch(npx)) return s;

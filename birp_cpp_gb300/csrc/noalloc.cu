@@ -32,7 +32,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 unsigned char* g_scratch_addr[kMaxDevices] = {};
-int g_grid[kMaxDevices] = {};
+int g_grid[kMaxDevices][2] = {};  // persistent grid per kernel class
 
 // Host staging of the request table (pageable host memory; cudaMemcpyAsync
 // returns once it has been read, so the lock covers only the copy).
@@ -40,15 +40,16 @@ std::mutex g_stage_mu;
 alignas(16) unsigned char g_stage[kOffCounter];
 
 // Once per device, with that device current: the device address of the
-// scratch array and the persistent grid size.
-birp_status setup_device(int dev, unsigned char** addr, int* grid) {
+// scratch array and the persistent grid size of each kernel class.
+birp_status setup_device(int dev, unsigned char** addr, const int** grid) {
   std::lock_guard<std::mutex> lk(g_setup_mu);
   if (!g_scratch_addr[dev]) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
     g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-    g_grid[dev] = persistent_grid(BATCH_ANY);
+    g_grid[dev][BATCH_CUBE_TRI] = persistent_grid(BATCH_CUBE_TRI);
+    g_grid[dev][BATCH_ANY] = persistent_grid(BATCH_ANY);
   }
   *addr = g_scratch_addr[dev];
   *grid = g_grid[dev];
@@ -71,7 +72,7 @@ extern "C" birp_status birp_batch_render_noalloc(const birp_request* reqs, int n
   if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return fail(BIRP_ERR_INVALID, "device %d out of range", dev);
   unsigned char* scratch = nullptr;
-  int grid = 0;
+  const int* grid = nullptr;
   if (birp_status s = setup_device(dev, &scratch, &grid)) return s;
   cudaStream_t st = stream ? (cudaStream_t)stream : (g_ctx.device == dev ? g_ctx.stream : (cudaStream_t)0);
 
@@ -80,9 +81,13 @@ extern "C" birp_status birp_batch_render_noalloc(const birp_request* reqs, int n
   int* first = reinterpret_cast<int*>(g_stage + kOffFirst);
   int* order = reinterpret_cast<int*>(g_stage + kOffOrder);
   RequestDev* rq = reinterpret_cast<RequestDev*>(g_stage + kOffReqs);
+  // one launch: the trilinear-cube kernel when every request is one, else
+  // the general kernel
+  int cls = BATCH_CUBE_TRI;
   for (int i = 0; i < n; ++i) {
     if (!outs_device[i]) return fail(BIRP_ERR_INVALID, "output %d is NULL", i);
     if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, reqs[i].cam, outs_device[i], rq[i])) return s;
+    if (reqs[i].cmem || !reqs[i].cam.trilinear) cls = BATCH_ANY;
   }
   // largest work first (as the allocating batch path)
   for (int i = 0; i < n; ++i) order[i] = i;
@@ -106,7 +111,7 @@ extern "C" birp_status birp_batch_render_noalloc(const birp_request* reqs, int n
   if ((e = cudaMemsetAsync(scratch + kOffCounter, 0, sizeof(unsigned int), st)) != cudaSuccess ||
       (e = cudaMemcpyAsync(scratch, g_stage, kOffReqs + (size_t)n * sizeof(RequestDev), cudaMemcpyHostToDevice,
                            st)) != cudaSuccess ||
-      (e = launch_render_batch(bd, grid, st)) != cudaSuccess)
+      (e = launch_render_batch(bd, grid[cls], st, cls)) != cudaSuccess)
     return fail(BIRP_ERR_CUDA, "no-allocation batch: %s", cudaGetErrorString(e));
   return ok();
 }
