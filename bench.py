@@ -217,9 +217,10 @@ def run_c4(args, B):
              for g, r0 in enumerate(r0_groups)]
     build.build()
     B.init(0)
+    layout = B.CUBE_COMPACT if args.c4_layout == "compact" else B.CUBE_RECORDS
     srv = B.Server(B.server_config(cube_budget_bytes=int(args.c4_budget_gb * (1 << 30)), slots=3,
                                    max_batch_requests=64, max_batch_pixels=16 << 20, max_wait_ms=1.0,
-                                   max_queue=1 << 16))
+                                   max_queue=1 << 16, cube_layout=layout))
     ids = []
     for i in range(args.c4_cubes):
         base = bases[i % len(bases)]
@@ -259,15 +260,16 @@ def run_c4(args, B):
                         "hits": st1.cube_hits - st0.cube_hits, "rejected": st1.rejected - st0.rejected})
         print(json.dumps(results[-1]), flush=True)
     srv.close()
-    # plain per-call latency on one resident cube
-    cube = B.Cube(xs, ys, zs, bases[0])
+    # plain per-call latency on one resident cube of the same layout
+    cube = B.Cube(xs, ys, zs, bases[0], layout=layout)
     pl = []
     for c in cams[:200]:
         t = time.perf_counter()
         B.render(cube, c, out=bufs[0][: c.nx * c.ny].reshape(c.ny, c.nx))
         pl.append(1000 * (time.perf_counter() - t))
     print(json.dumps({"workload": f"config 4 serving sweep: {args.c4_cubes} cubes of {nx}x{ny}x{nz}, Zipf(1.1), "
-                                  f"{args.c4_budget_gb} GB budget, {args.c4_seconds} s per rate",
+                                  f"{args.c4_budget_gb} GB budget, {args.c4_seconds} s per rate, "
+                                  f"{args.c4_layout} layout",
                       "sweep": results, "plain_p50_ms": float(np.percentile(pl, 50)),
                       "plain_p99_ms": float(np.percentile(pl, 99)), "plain_images_s": len(pl) / (sum(pl) / 1000)}))
 
@@ -368,6 +370,8 @@ def main():
     ap.add_argument("--c4-budget-gb", type=float, default=60.0)
     ap.add_argument("--c4-rates", default="50,200,500,1000,2000")
     ap.add_argument("--c4-seconds", type=float, default=10.0)
+    ap.add_argument("--c4-layout", default="compact", choices=["compact", "records"],
+                    help="device layout of the served cubes")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.impl == "reference":
@@ -538,9 +542,10 @@ def main():
             "ray_samples_per_s": samples_per_step * world / (step_ms / 1000.0),
             "roofline": roofline, "roofline_per_sample": roofline_per_sample, "roofline_hbm": roofline_hbm,
             "cpu_baseline": cpu, "parity": parity,
-            # each step replays one graph with two kernels: the general one
-            # (no work here) and the trilinear-cube one
-            "gpu_launches": 2 * args.steps, "clocks": clocks.summary(),
+            # each step replays one graph with three kernels: the general one
+            # and the compact-layout one (no work here) and the records-layout
+            # trilinear one
+            "gpu_launches": 3 * args.steps, "clocks": clocks.summary(),
             "exact_fp64_rays_per_step": ks["exact_range_rays"] / args.steps,
             "samples_per_cell": (ks["samples"] / ks["cells"]) if ks.get("cells") else None,
         }

@@ -22,6 +22,11 @@ namespace birp {
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+int request_class(const birp_request& r) {
+  if (r.cmem || !r.cam.trilinear) return BATCH_ANY;
+  return (r.cube && r.cube->layout == BIRP_CUBE_COMPACT) ? BATCH_CUBE_TRI_COMPACT : BATCH_CUBE_TRI;
+}
+
 static void free_batch(birp_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
@@ -46,13 +51,13 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   birp_batch* b = new birp_batch();
   b->max_req = max_requests;
   b->max_px = max_pixels;
-  // staging block: hdr[2][4] | first[2][max+1] | order[2][max] | (16B aligned) RequestDev[max]
-  size_t off = 8 * sizeof(int);
-  for (int c = 0; c < 2; ++c) {
+  // staging block: hdr[C][4] | first[C][max+1] | order[C][max] | (16B aligned) RequestDev[max]
+  size_t off = 4 * BATCH_CLASSES * sizeof(int);
+  for (int c = 0; c < BATCH_CLASSES; ++c) {
     b->off_first[c] = off;
     off += (size_t)(max_requests + 1) * sizeof(int);
   }
-  for (int c = 0; c < 2; ++c) {
+  for (int c = 0; c < BATCH_CLASSES; ++c) {
     b->off_order[c] = off;
     off += (size_t)max_requests * sizeof(int);
   }
@@ -66,7 +71,7 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaHostAlloc(&b->h_stage, b->stage_bytes, cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaMalloc(&b->d_stage, b->stage_bytes)) != cudaSuccess ||
-      (e = cudaMalloc(&b->d_counter, 2 * sizeof(unsigned int))) != cudaSuccess ||
+      (e = cudaMalloc(&b->d_counter, BATCH_CLASSES * sizeof(unsigned int))) != cudaSuccess ||
       (e = cudaMalloc(&b->d_out, (size_t)max_pixels * sizeof(float))) != cudaSuccess ||
       (e = cudaHostAlloc(&b->h_out, (size_t)max_pixels * sizeof(float), cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaEventCreate(&b->e_start)) != cudaSuccess || (e = cudaEventCreate(&b->e_kernel)) != cudaSuccess ||
@@ -75,12 +80,13 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
                      cudaGetErrorString(e)));
   std::memset(b->h_stage, 0, b->stage_bytes);
 
-  // One graph: descriptors H2D, both queue heads reset, then the general
+  // One graph: descriptors H2D, the queue heads reset, then the general
   // kernel (CMEM and nearest requests: few but heavy, so they start first)
-  // and the trilinear-cube kernel (64 registers, full occupancy). A class
-  // with no requests costs one launch whose CTAs exit at once.
-  BatchDev bd[2];
-  for (int c = 0; c < 2; ++c) {
+  // and the two trilinear-cube kernels (compact, then records layout; 64
+  // registers, full occupancy). A class with no requests costs one launch
+  // whose CTAs exit at once.
+  BatchDev bd[BATCH_CLASSES];
+  for (int c = 0; c < BATCH_CLASSES; ++c) {
     bd[c].hdr = reinterpret_cast<const int*>(b->d_stage) + 4 * c;
     bd[c].first = reinterpret_cast<const int*>(b->d_stage + b->off_first[c]);
     bd[c].order = reinterpret_cast<const int*>(b->d_stage + b->off_order[c]);
@@ -92,9 +98,8 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   if ((e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
   cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
-  cudaMemsetAsync(b->d_counter, 0, 2 * sizeof(unsigned int), b->stream);
-  launch_render_batch(bd[BATCH_ANY], b->grid[BATCH_ANY], b->stream, BATCH_ANY);
-  launch_render_batch(bd[BATCH_CUBE_TRI], b->grid[BATCH_CUBE_TRI], b->stream, BATCH_CUBE_TRI);
+  cudaMemsetAsync(b->d_counter, 0, BATCH_CLASSES * sizeof(unsigned int), b->stream);
+  for (int c : {BATCH_ANY, BATCH_CUBE_TRI_COMPACT, BATCH_CUBE_TRI}) launch_render_batch(bd[c], b->grid[c], b->stream, c);
   e = cudaStreamEndCapture(b->stream, &b->graph);
   if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
   if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess)
@@ -115,7 +120,7 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* 
   b->npx.assign(n, 0);
   int64_t used = 0;
   std::vector<double> work(n);
-  std::vector<int> members[2];
+  std::vector<int> members[BATCH_CLASSES];
   for (int i = 0; i < n; ++i) {
     const birp_camera& c = reqs[i].cam;
     if (birp_status s = validate_camera(&c)) return s;
@@ -128,11 +133,11 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* 
     if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, out, rq[i])) return s;
     used += npx;
     work[i] = (double)npx * c.n_samples * (reqs[i].cmem ? 16.0 : 1.0);
-    members[(reqs[i].cmem || !c.trilinear) ? BATCH_ANY : BATCH_CUBE_TRI].push_back(i);
+    members[request_class(reqs[i])].push_back(i);
   }
   // per class: largest work first, so long renders start early and small
   // ones fill the tail
-  for (int cls = 0; cls < 2; ++cls) {
+  for (int cls = 0; cls < BATCH_CLASSES; ++cls) {
     int* first = reinterpret_cast<int*>(b->h_stage + b->off_first[cls]);
     int* order = reinterpret_cast<int*>(b->h_stage + b->off_order[cls]);
     std::vector<int>& m = members[cls];

@@ -7,9 +7,11 @@
 struct birp_batch {
   int max_req = 0;
   int64_t max_px = 0;
-  // staging block: hdr[2][4] | first[2][max+1] | order[2][max] | (16 B aligned)
-  // RequestDev[max]; class c's tables describe its share of the requests
-  size_t off_first[2] = {0, 0}, off_order[2] = {0, 0}, off_reqs = 0, stage_bytes = 0;
+  // staging block: hdr[C][4] | first[C][max+1] | order[C][max] | (16 B
+  // aligned) RequestDev[max] for the C = BATCH_CLASSES kernel classes; class
+  // c's tables describe its share of the requests
+  size_t off_first[birp::BATCH_CLASSES] = {}, off_order[birp::BATCH_CLASSES] = {};
+  size_t off_reqs = 0, stage_bytes = 0;
   char* h_stage = nullptr;   // pinned descriptors of the next launch
   char* d_stage = nullptr;
   unsigned int* d_counter = nullptr;  // work queue heads, one per kernel class
@@ -19,17 +21,19 @@ struct birp_batch {
   std::vector<int64_t> npx;
   int n = 0;
   int64_t used = 0;
-  int grid[2] = {0, 0};
+  int grid[birp::BATCH_CLASSES] = {};
   bool pending = false;
   bool direct = false;       // the last launch wrote the caller's host images itself
   cudaStream_t stream = nullptr;
-  // {descriptors H2D, queue heads reset, general kernel, trilinear kernel}
+  // {descriptors H2D, queue heads reset, the kernels of the classes}
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaEvent_t e_start = nullptr, e_kernel = nullptr, e_end = nullptr;
 };
 
 namespace birp {
+// the persistent-kernel class (BatchClass) that renders a request
+int request_class(const birp_request& r);
 birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out);
 // direct_outs: when given, request i's image is written by the kernel into
 // direct_outs[i] (host memory the device can write) and nothing is copied back

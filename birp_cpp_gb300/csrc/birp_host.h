@@ -22,6 +22,9 @@ struct birp_cube {
   double* d_c64 = nullptr;      // 3 axes, concatenated
   float4* d_lut = nullptr;
   float2* d_cells = nullptr;    // walk tables (up and down) of the 3 axes, concatenated
+  int layout = BIRP_CUBE_RECORDS;
+  float* d_grid = nullptr;      // compact layout: padded node values
+  float4* d_walk4 = nullptr;    // compact layout: walk tables with inverse widths
   size_t device_bytes = 0;
   cudaStream_t alloc_stream = nullptr;  // non-null: stream-ordered (pool) allocations
 };
@@ -78,6 +81,7 @@ cudaStream_t pick_stream(void* s);
 
 // cube.cu
 birp_status analyze_axis(const double* c, int n, char name, birp_cube& cube, int k);
+// builds the device form of cube.layout (cube.n, cube.c, ... already set)
 birp_status upload_cube(birp_cube& cube, const float* values, cudaStream_t stream, bool stream_alloc);
 // estimate of the device bytes a cube of these dims will hold
 size_t cube_device_bytes(const birp_cube& cube);

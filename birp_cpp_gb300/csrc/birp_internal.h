@@ -17,6 +17,12 @@
 //    cell order, for rays moving down (exit plane c_k), so a ray always walks
 //    its table forward. The guard cells' exit planes are +inf / -inf, which
 //    ends the walk at the box edge.
+//  * compact layout (a cube-creation option for memory-bound uses such as
+//    serving many cubes under a byte budget): instead of the records, the
+//    FP32 node values with one guard node each side ((nx+2)(ny+2)(nz+2),
+//    about 1x the input), the march forming a cell's coefficients from its
+//    8 corners in FP32, and float4 walk tables {base, exit plane, 1/width, 0}
+//    (1/width = 0 at guard cells).
 //  * per-axis index tables (LUT) for nonuniform axes: float4 bins of width at
 //    most the smallest cell, each holding one piecewise-linear index map.
 //  * FP64 axis coordinates, read only by the exact (FP64) decisions.
@@ -54,6 +60,14 @@ struct CubeDev {
   // entries, j in [-1, n-1]
   const float2* walk_up[3];
   const float2* walk_dn[3];
+  // compact layout (rec == nullptr): padded node values and their strides,
+  // and the float4 walk tables (same indexing as walk_up / walk_dn)
+  int compact;
+  const float* grid;
+  uint32_t gx;          // nx + 2
+  uint32_t gxy;         // (nx + 2) * (ny + 2)
+  const float4* walk4_up[3];
+  const float4* walk4_dn[3];
 };
 
 // CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
@@ -86,6 +100,7 @@ struct RequestDev {
   int tiles_x;       // tiles along x for this request's tile shape
   int tiles;         // total tiles
   int axes_lut;      // cube: 1 when any axis needs the LUT
+  int compact;       // cube: 1 in the compact layout (node values, no records)
   const CubeDev* cube;   // device pointer (kind == SPACE_CUBE)
   const CmemDev* cmem;   // device pointer (kind == SPACE_CMEM)
   float* out;            // ny*nx floats, row 0 = top
@@ -120,7 +135,10 @@ struct BatchDev {
 cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaStream_t stream);
 // Persistent batch kernel classes: CUBE_TRI renders only trilinear cube
 // requests (fewer registers, more resident warps); ANY renders every kind.
-enum BatchClass : int { BATCH_CUBE_TRI = 0, BATCH_ANY = 1 };
+// Persistent-kernel classes of a batch: trilinear cube requests in the
+// records layout, the same in the compact layout, and everything else (CMEM,
+// nearest mode) in the general kernel.
+enum BatchClass : int { BATCH_CUBE_TRI = 0, BATCH_ANY = 1, BATCH_CUBE_TRI_COMPACT = 2, BATCH_CLASSES = 3 };
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);

@@ -226,6 +226,7 @@ birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const bi
   if (cube) {
     r.cube = cube->d_desc;
     r.axes_lut = cube->h_desc.all_uniform ? 0 : 1;
+    r.compact = cube->h_desc.compact;
     for (int k = 0; k < 3; ++k)
       r.oidx[k] = cube->uniform[k] ? (float)((c.pos[k] - cube->c[k][0]) * cube->inv_h[k]) : 0.f;
   } else {
@@ -364,12 +365,20 @@ void birp_shutdown(void) {
 
 birp_status birp_cube_create(const double* xs, int nx, const double* ys, int ny, const double* zs, int nz,
                              const float* values, birp_cube** out) {
+  return birp_cube_create_layout(xs, nx, ys, ny, zs, nz, values, BIRP_CUBE_RECORDS, out);
+}
+
+birp_status birp_cube_create_layout(const double* xs, int nx, const double* ys, int ny, const double* zs, int nz,
+                                    const float* values, int layout, birp_cube** out) {
   if (birp_status s = check_init()) return s;
   if (!out || !values || !xs || !ys || !zs) return fail(BIRP_ERR_INVALID, "NULL argument");
+  if (layout != BIRP_CUBE_RECORDS && layout != BIRP_CUBE_COMPACT)
+    return fail(BIRP_ERR_INVALID, "unknown cube layout %d", layout);
   *out = nullptr;
   const double* axes[3] = {xs, ys, zs};
   const int n[3] = {nx, ny, nz};
   birp_cube* c = new birp_cube();
+  c->layout = layout;
   for (int k = 0; k < 3; ++k) {
     birp_status s = analyze_axis(axes[k], n[k], "xyz"[k], *c, k);
     if (s) {
@@ -408,6 +417,7 @@ birp_status birp_cube_get_info(const birp_cube* cube, birp_cube_info* info) {
   info->nz = cube->n[2];
   for (int k = 0; k < 3; ++k) info->uniform[k] = cube->uniform[k];
   info->device_bytes = cube->device_bytes;
+  info->layout = cube->layout;
   return ok();
 }
 

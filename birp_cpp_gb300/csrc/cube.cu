@@ -82,15 +82,16 @@ birp_status ensure_xyz_scratch(size_t floats) {
 void destroy_cube_device(birp_cube& c) {
   if (c.alloc_stream) {
     // stream-ordered pool memory: no device-wide synchronisation on release
-    for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells})
+    for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
+                    (void*)c.d_grid, (void*)c.d_walk4})
       if (p) cudaFreeAsync(p, c.alloc_stream);
   } else {
-    if (c.d_vals) cudaFree(c.d_vals);
-    if (c.d_c64) cudaFree(c.d_c64);
-      if (c.d_lut) cudaFree(c.d_lut);
-    if (c.d_desc) cudaFree(c.d_desc);
-    if (c.d_cells) cudaFree(c.d_cells);
+    for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
+                    (void*)c.d_grid, (void*)c.d_walk4})
+      if (p) cudaFree(p);
   }
+  c.d_grid = nullptr;
+  c.d_walk4 = nullptr;
   c.d_cells = nullptr;
   c.d_vals = nullptr;
   c.d_c64 = nullptr;
@@ -136,39 +137,55 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   }
 
   size_t coords = (size_t)nx + ny + nz;
-  // walk tables of every axis, {base, exit plane} per cell -1..n-1: the up
-  // table in cell order, then the down table in reverse cell order. Guard
-  // cells take the edge node as base (their coefficients along the axis are
-  // 0) and an infinite exit plane, so the walk stops there.
-  std::vector<float2> walk;
+  // walk tables of every axis, per cell -1..n-1: the up table in cell order,
+  // then the down table in reverse cell order. Guard cells take the edge node
+  // as base (their coefficients along the axis are 0) and an infinite exit
+  // plane, so the walk stops there. Records layout: float2 {base, exit
+  // plane}; compact layout: float4 {base, exit plane, 1/width (0 at guard
+  // cells), 0}. One padding entry at the end: a walk that reads one entry
+  // ahead of its cell may read one past the last table's guard cell (the
+  // value is never used).
+  const bool compact = c.layout == BIRP_CUBE_COMPACT;
+  std::vector<float4> walk;
   walk.reserve(2 * (coords + 3) + 1);
   size_t up_off[3], dn_off[3];
   for (int k = 0; k < 3; ++k) {
     const std::vector<double>& ck = c.c[k];
     const int n = c.n[k];
-    walk.push_back(make_float2((float)ck[0], (float)ck[0]));  // cell -1
+    auto iw = [&](int j) { return (float)(1.0 / (ck[j + 1] - ck[j])); };
+    walk.push_back(make_float4((float)ck[0], (float)ck[0], 0.f, 0.f));  // cell -1
     up_off[k] = walk.size();
-    for (int j = 0; j + 1 < n; ++j) walk.push_back(make_float2((float)ck[j], (float)ck[j + 1]));
-    walk.push_back(make_float2((float)ck[n - 1], INFINITY));  // cell n-1
-    walk.push_back(make_float2((float)ck[n - 1], (float)ck[n - 1]));  // cell n-1
-    for (int j = n - 2; j >= 0; --j) walk.push_back(make_float2((float)ck[j], (float)ck[j]));
+    for (int j = 0; j + 1 < n; ++j) walk.push_back(make_float4((float)ck[j], (float)ck[j + 1], iw(j), 0.f));
+    walk.push_back(make_float4((float)ck[n - 1], INFINITY, 0.f, 0.f));  // cell n-1
+    walk.push_back(make_float4((float)ck[n - 1], (float)ck[n - 1], 0.f, 0.f));  // cell n-1
+    for (int j = n - 2; j >= 0; --j) walk.push_back(make_float4((float)ck[j], (float)ck[j], iw(j), 0.f));
     dn_off[k] = walk.size() - 1;  // cell 0
-    walk.push_back(make_float2((float)ck[0], -INFINITY));  // cell -1
+    walk.push_back(make_float4((float)ck[0], -INFINITY, 0.f, 0.f));  // cell -1
   }
-  // one padding entry: a walk that reads one entry ahead of its cell may
-  // read one past the last table's guard cell (the value is never used)
-  walk.push_back(make_float2(0.f, 0.f));
-  CKU(dev_alloc(&c.d_cells, walk.size() * sizeof(float2), c.alloc_stream));
+  walk.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
+  std::vector<float2> walk2;
+  if (!compact) {
+    walk2.reserve(walk.size());
+    for (const float4& w : walk) walk2.push_back(make_float2(w.x, w.y));
+  }
   const size_t records = ((size_t)nx + 1) * ((size_t)ny + 1) * ((size_t)nz + 1);
-  CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
-  float* scalar = nullptr;  // the padded scalar grid, turned into cell records then freed
+  // the padded scalar grid; records layout: turned into records, then freed
+  // (held in d_grid until then, so a failed upload releases it with the rest)
+  float* scalar = nullptr;
   CKU(dev_alloc(&scalar, total * sizeof(float), c.alloc_stream));
+  c.d_grid = scalar;
+  if (compact) {
+    CKU(dev_alloc(&c.d_walk4, walk.size() * sizeof(float4), c.alloc_stream));
+  } else {
+    CKU(dev_alloc(&c.d_cells, walk2.size() * sizeof(float2), c.alloc_stream));
+    CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
+  }
   CKU(dev_alloc(&c.d_c64, coords * sizeof(double), c.alloc_stream));
   if (!lut.empty()) CKU(dev_alloc(&c.d_lut, lut.size() * sizeof(float4), c.alloc_stream));
   CKU(dev_alloc(&c.d_desc, sizeof(CubeDev), c.alloc_stream));
-  c.device_bytes = records * 2 * sizeof(float4) + coords * sizeof(double) + lut.size() * sizeof(float4) +
-                   walk.size() * sizeof(float2) +
-                   sizeof(CubeDev);
+  c.device_bytes = coords * sizeof(double) + lut.size() * sizeof(float4) + sizeof(CubeDev) +
+                   (compact ? total * sizeof(float) + walk.size() * sizeof(float4)
+                            : records * 2 * sizeof(float4) + walk2.size() * sizeof(float2));
 
   // interior values: one strided 3D copy from the caller's x-fastest array
   cudaMemcpy3DParms p;
@@ -185,11 +202,17 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   all.reserve(coords);
   for (int k = 0; k < 3; ++k) all.insert(all.end(), c.c[k].begin(), c.c[k].end());
   CKU(cudaMemcpyAsync(c.d_c64, all.data(), coords * sizeof(double), cudaMemcpyHostToDevice, st));
-  CKU(launch_cube_records(scalar, nx, ny, nz, c.d_c64, c.d_c64 + nx, c.d_c64 + nx + ny, c.d_vals, st));
-  if (c.alloc_stream) CKU(cudaFreeAsync(scalar, st));
-
+  if (compact) {
+    CKU(cudaMemcpyAsync(c.d_walk4, walk.data(), walk.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+  } else {
+    CKU(launch_cube_records(scalar, nx, ny, nz, c.d_c64, c.d_c64 + nx, c.d_c64 + nx + ny, c.d_vals, st));
+    if (c.alloc_stream) {
+      c.d_grid = nullptr;
+      CKU(cudaFreeAsync(scalar, st));
+    }
+    CKU(cudaMemcpyAsync(c.d_cells, walk2.data(), walk2.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+  }
   if (!lut.empty()) CKU(cudaMemcpyAsync(c.d_lut, lut.data(), lut.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CKU(cudaMemcpyAsync(c.d_cells, walk.data(), walk.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
 
   size_t off = 0;
   for (int k = 0; k < 3; ++k) {
@@ -212,13 +235,25 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   d.cx = (uint32_t)(nx + 1);
   d.cxy = (uint32_t)((nx + 1) * (ny + 1));
   d.lut = c.d_lut;
+  d.compact = compact ? 1 : 0;
+  d.grid = compact ? c.d_grid : nullptr;
+  d.gx = (uint32_t)px;
+  d.gxy = (uint32_t)(px * py);
   for (int k = 0; k < 3; ++k) {
-    d.walk_up[k] = c.d_cells + up_off[k];
-    d.walk_dn[k] = c.d_cells + dn_off[k];
+    if (compact) {
+      d.walk4_up[k] = c.d_walk4 + up_off[k];
+      d.walk4_dn[k] = c.d_walk4 + dn_off[k];
+    } else {
+      d.walk_up[k] = c.d_cells + up_off[k];
+      d.walk_dn[k] = c.d_cells + dn_off[k];
+    }
   }
   CKU(cudaMemcpyAsync(c.d_desc, &d, sizeof d, cudaMemcpyHostToDevice, st));
   CKU(cudaStreamSynchronize(st));
-  if (!c.alloc_stream) CKU(cudaFree(scalar));
+  if (!compact && !c.alloc_stream) {
+    c.d_grid = nullptr;
+    CKU(cudaFree(scalar));
+  }
   return BIRP_OK;
 }
 
@@ -233,8 +268,10 @@ size_t cube_device_bytes(const birp_cube& c) {
   if (!all_uniform)
     for (int k = 0; k < 3; ++k)
       lut += (size_t)std::max(1.0, std::ceil((c.c[k].back() - c.c[k].front()) / c.min_gap[k])) * sizeof(float4);
-  const size_t cells = (2 * (coords + 3) + 1) * sizeof(float2);
+  const size_t walk = 2 * (coords + 3) + 1;
   const size_t records = ((size_t)c.n[0] + 1) * ((size_t)c.n[1] + 1) * ((size_t)c.n[2] + 1);
-  return records * 2 * sizeof(float4) + coords * sizeof(double) + lut + cells + sizeof(CubeDev);
+  const size_t layout_bytes = c.layout == BIRP_CUBE_COMPACT ? total * sizeof(float) + walk * sizeof(float4)
+                                                            : records * 2 * sizeof(float4) + walk * sizeof(float2);
+  return layout_bytes + coords * sizeof(double) + lut + sizeof(CubeDev);
 }
 }  // namespace birp

@@ -12,6 +12,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "batch.h"
 #include "birp_host.h"
 
 namespace birp {
@@ -32,7 +33,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 unsigned char* g_scratch_addr[kMaxDevices] = {};
-int g_grid[kMaxDevices][2] = {};  // persistent grid per kernel class
+int g_grid[kMaxDevices][BATCH_CLASSES] = {};  // persistent grid per kernel class
 
 // Host staging of the request table (pageable host memory; cudaMemcpyAsync
 // returns once it has been read, so the lock covers only the copy).
@@ -48,8 +49,7 @@ birp_status setup_device(int dev, unsigned char** addr, const int** grid) {
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
     g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-    g_grid[dev][BATCH_CUBE_TRI] = persistent_grid(BATCH_CUBE_TRI);
-    g_grid[dev][BATCH_ANY] = persistent_grid(BATCH_ANY);
+    for (int c = 0; c < BATCH_CLASSES; ++c) g_grid[dev][c] = persistent_grid(c);
   }
   *addr = g_scratch_addr[dev];
   *grid = g_grid[dev];
@@ -81,13 +81,13 @@ extern "C" birp_status birp_batch_render_noalloc(const birp_request* reqs, int n
   int* first = reinterpret_cast<int*>(g_stage + kOffFirst);
   int* order = reinterpret_cast<int*>(g_stage + kOffOrder);
   RequestDev* rq = reinterpret_cast<RequestDev*>(g_stage + kOffReqs);
-  // one launch: the trilinear-cube kernel when every request is one, else
-  // the general kernel
-  int cls = BATCH_CUBE_TRI;
+  // one launch: a trilinear-cube kernel when every request is of its class,
+  // else the general kernel
+  int cls = n > 0 ? request_class(reqs[0]) : BATCH_ANY;
   for (int i = 0; i < n; ++i) {
     if (!outs_device[i]) return fail(BIRP_ERR_INVALID, "output %d is NULL", i);
     if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, reqs[i].cam, outs_device[i], rq[i])) return s;
-    if (reqs[i].cmem || !reqs[i].cam.trilinear) cls = BATCH_ANY;
+    if (request_class(reqs[i]) != cls) cls = BATCH_ANY;
   }
   // largest work first (as the allocating batch path)
   for (int i = 0; i < n; ++i) order[i] = i;

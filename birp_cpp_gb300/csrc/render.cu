@@ -25,6 +25,7 @@
 //    floor uses the magic-constant trick (no conversion-pipe instructions).
 #include <algorithm>
 #include <cstdint>
+#include <type_traits>
 
 #include "birp_internal.h"
 #include "cell_index.h"
@@ -318,7 +319,8 @@ enum Interp { NEAREST = 0, TRILINEAR = 1 };
 // Axis handling of the cube march: UNIFORM computes the index affinely, LUT
 // through the index tables, DDA walks cell by cell along the ray (any axes;
 // trilinear only).
-enum Axes { AXES_UNIFORM = 0, AXES_LUT = 1, AXES_DDA = 2 };
+// AXES_DDA_COMPACT is the same walk over a compact-layout cube.
+enum Axes { AXES_UNIFORM = 0, AXES_LUT = 1, AXES_DDA = 2, AXES_DDA_COMPACT = 3 };
 
 // One pixel tile of one request. The lanes-per-ray split S = 2^seg_log2 is a
 // runtime value of the request (it only sets the tile shape, the lane -> ray
@@ -439,7 +441,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   const float fS = (float)S;
 
   int nsamp = iters;  // samples this lane evaluates (for the counters)
-  if constexpr (KIND == SPACE_CUBE && AXES == AXES_DDA) {
+  if constexpr (KIND == SPACE_CUBE && (AXES == AXES_DDA || AXES == AXES_DDA_COMPACT)) {
+    constexpr bool COMPACT = AXES == AXES_DDA_COMPACT;
     // Cell-space integration. A lane takes a contiguous run of its ray's
     // samples and walks the cells the run crosses. Per axis the sample
     // position relative to the current cell's base node is affine in the
@@ -464,10 +467,15 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     // per axis: position step st, its reciprocal, position at the run's first
     // sample, the run's first position relative to the current cell's base
     // node (xb), the exit index ex, the walk-table pointer and the record step
+    // (compact layout: the inverse width iw of the current cell and the
+    // pointer g to its lower corner node instead of the record pointer q)
+    using WalkEntry = std::conditional_t<COMPACT, float4, float2>;
     float st[3], rst[3], bs[3], xb[3], ex[3];
-    const float2* wt[3];
+    [[maybe_unused]] float iw[3];
+    const WalkEntry* wt[3];
     int dstr[3];
     const float4* q = C.rec;
+    [[maybe_unused]] const float* g = C.grid;
     if (count > 0) {
       const float f0 = (float)first_c;
       int k0s[3];
@@ -484,15 +492,24 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         // direction from the sign bit: a zero step of either sign (rst =
         // +-inf) then gives an exit index of +inf (or NaN), never a crossing
         const bool up = !signbit(d32[k]);
-        wt[k] = up ? C.walk_up[k] + k0s[k] : C.walk_dn[k] - k0s[k];
-        const float2 e = __ldg(wt[k]);  // {base node, exit plane}
+        if constexpr (COMPACT) wt[k] = up ? C.walk4_up[k] + k0s[k] : C.walk4_dn[k] - k0s[k];
+        else wt[k] = up ? C.walk_up[k] + k0s[k] : C.walk_dn[k] - k0s[k];
+        const WalkEntry e = __ldg(wt[k]);  // {base node, exit plane[, 1/width]}
         xb[k] = bs[k] - e.x;
         // exit index of the cell along this axis: bs + ex * st = exit plane
         ex[k] = (e.y - bs[k]) * rst[k];
-        const int stride = (int)record_stride(C.cx, C.cxy, k);
-        dstr[k] = 2 * (up ? stride : -stride);
+        if constexpr (COMPACT) {
+          iw[k] = e.z;
+          const int stride = (int)record_stride(C.gx, C.gxy, k);  // in nodes
+          dstr[k] = up ? stride : -stride;
+        } else {
+          const int stride = (int)record_stride(C.cx, C.cxy, k);  // in records; 2 float4 each
+          dstr[k] = 2 * (up ? stride : -stride);
+        }
       }
-      q = C.rec + 2 * record_index(C.cx, C.cxy, k0s[0], k0s[1], k0s[2]);
+      if constexpr (COMPACT) g = C.grid + record_index(C.gx, C.gxy, k0s[0], k0s[1], k0s[2]);
+      else q = C.rec + 2 * record_index(C.cx, C.cxy, k0s[0], k0s[1], k0s[2]);
+      [[maybe_unused]] const int gx = (int)C.gx, gxy = (int)C.gxy;
       // the ray's step products, the same in every cell (local coordinates
       // are physical offsets)
       const float DxDy = st[0] * st[1], DxDz = st[0] * st[2], DyDz = st[1] * st[2];
@@ -502,7 +519,24 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       const int cap = count + C.ax[0].n + C.ax[1].n + C.ax[2].n + 4;
       int ncell = 0;
       for (int guard = 0; u < ub && guard < cap; ++guard) {
-        const float4 lo = __ldg(q), hi = __ldg(q + 1);  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
+        float4 lo, hi;  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
+        if constexpr (COMPACT) {
+          // the cell's trilinear coefficients from its 8 corners, in local
+          // physical coordinates (scaled by the inverse widths)
+          const float v000 = __ldg(g), v001 = __ldg(g + 1), v010 = __ldg(g + gx), v011 = __ldg(g + gx + 1);
+          const float v100 = __ldg(g + gxy), v101 = __ldg(g + gxy + 1), v110 = __ldg(g + gxy + gx),
+                      v111 = __ldg(g + gxy + gx + 1);
+          const float d1 = v001 - v000, d2 = v010 - v000, d3 = v100 - v000;
+          const float t = v011 - v010, w = v101 - v100;
+          const float e4 = t - d1, e5 = w - d1, e6 = (v110 - v100) - d2;
+          const float e7 = ((v111 - v110) - w) - e4;
+          const float ixy = iw[0] * iw[1];
+          lo = make_float4(v000, d1 * iw[0], d2 * iw[1], e4 * ixy);
+          hi = make_float4(d3 * iw[2], e5 * (iw[0] * iw[2]), e6 * (iw[1] * iw[2]), e7 * (ixy * iw[2]));
+        } else {
+          lo = __ldg(q);
+          hi = __ldg(q + 1);
+        }
         const float nxt = fminf(ceilf(fminf(fminf(ex[0], ex[1]), ex[2])), ub);
         if (nxt > u) {
           const float m = nxt - u;
@@ -534,10 +568,15 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         for (int k = 0; k < 3; ++k) {
           while (ex[k] <= u) {
             ++wt[k];
-            const float2 e = __ldg(wt[k]);
+            const WalkEntry e = __ldg(wt[k]);
             xb[k] = bs[k] - e.x;
             ex[k] = (e.y - bs[k]) * rst[k];
-            q += dstr[k];
+            if constexpr (COMPACT) {
+              iw[k] = e.z;
+              g += dstr[k];
+            } else {
+              q += dstr[k];
+            }
           }
         }
       }
@@ -546,9 +585,12 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   } else if constexpr (KIND == SPACE_CUBE) {
     // nearest by truncation (UNIFORM / LUT index)
     const CubeDev& C = *R.cube;
-    // node k's value is the first corner of cell k's record
-    const float* __restrict__ vals = reinterpret_cast<const float*>(C.rec);
-    const int cxn = (int)C.cx, cxyn = (int)C.cxy;
+    // node k's value: the first corner of cell k's record (records layout,
+    // 8 floats per record) or the padded grid's node (compact layout)
+    const bool cmp = C.compact != 0;
+    const float* __restrict__ vals = cmp ? C.grid : reinterpret_cast<const float*>(C.rec);
+    const int cxn = cmp ? (int)C.gx : (int)C.cx, cxyn = cmp ? (int)C.gxy : (int)C.cxy;
+    const int vmul = cmp ? 1 : 8;
     const int hi0 = C.ax[0].n - 1, hi1 = C.ax[1].n - 1, hi2 = C.ax[2].n - 1;
     float st[3], bs[3];
 #pragma unroll
@@ -611,7 +653,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         }
         const int ix = min(max(bx - kMagicBits, -1), hi0), iy = min(max(by - kMagicBits, -1), hi1),
                   iz = min(max(bz - kMagicBits, -1), hi2);
-        v = __ldg(vals + 8 * record_index(cxn, cxyn, ix, iy, iz));
+        v = __ldg(vals + vmul * record_index(cxn, cxyn, ix, iy, iz));
       }
       acc.add(v);
       fi += fS;
@@ -679,7 +721,8 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
   if (R.kind == SPACE_CMEM) {
     render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM>(R, tx, ty, sm, st);
   } else if (R.interp) {
-    render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, st);
+    if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
+    else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, st);
   } else if (R.axes_lut) {
     render_tile<SPACE_CUBE, NEAREST, AXES_LUT>(R, tx, ty, sm, st);
   } else {
@@ -693,7 +736,7 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
 // first). CLS = BATCH_CUBE_TRI compiles only the trilinear cube march (fewer
 // registers, more resident warps); BATCH_ANY renders every request kind.
 template <int CLS>
-__global__ void __launch_bounds__(kThreads, CLS == BATCH_CUBE_TRI ? 8 : 1) render_batch_kernel(BatchDev B) {
+__global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY ? 1 : 8) render_batch_kernel(BatchDev B) {
   __shared__ TileSmem sm;
   __shared__ int s_item;
   const int n_reqs = __ldg(B.hdr), total_items = __ldg(B.hdr + 1);
@@ -716,6 +759,8 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_CUBE_TRI ? 8 : 1) rende
     const int tx = t % R.tiles_x, ty = t / R.tiles_x;
     if constexpr (CLS == BATCH_CUBE_TRI) {
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, B.stats);
+    } else if constexpr (CLS == BATCH_CUBE_TRI_COMPACT) {
+      render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
     } else {
       render_tile_any(R, tx, ty, sm, B.stats);
     }
@@ -796,7 +841,7 @@ __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int triline
     double p[3] = {(double)xyz[3 * t], (double)xyz[3 * t + 1], (double)xyz[3 * t + 2]};
     bool in = true;
     int k[3];
-    double f[3];
+    double f[3], w[3];
     for (int a = 0; a < 3; ++a) {
       const AxisDev& A = C.ax[a];
       if (!(A.c_first <= p[a] && p[a] < A.c_last)) {
@@ -811,9 +856,25 @@ __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int triline
       }
       k[a] = lo;
       f[a] = p[a] - A.c64[lo];  // local coordinate in the cell
+      w[a] = A.c64[lo + 1] - A.c64[lo];
     }
     if (!in) {
       out[t] = -1.f;
+      continue;
+    }
+    if (C.compact) {
+      // FP64 lerps x -> y -> z of the 8 corner nodes
+      const float* g = C.grid + record_index(C.gx, C.gxy, k[0], k[1], k[2]);
+      const long long gx = C.gx, gxy = C.gxy;
+      if (!trilinear) {
+        out[t] = g[0];
+        continue;
+      }
+      const double fx = f[0] / w[0], fy = f[1] / w[1], fz = f[2] / w[2];
+      auto lx = [&](long long o) { return (double)g[o] + fx * ((double)g[o + 1] - (double)g[o]); };
+      const double y0 = lx(0) + fy * (lx(gx) - lx(0));
+      const double y1 = lx(gxy) + fy * (lx(gxy + gx) - lx(gxy));
+      out[t] = (float)(y0 + fz * (y1 - y0));
       continue;
     }
     const float4* b = C.rec + 2 * record_index(C.cx, C.cxy, k[0], k[1], k[2]);
@@ -920,6 +981,8 @@ int tile_h(int segl2) { return th_of(segl2); }
 cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStream_t s) {
   dim3 grid((h.nx + tw_of(h.seg_log2) - 1) / tw_of(h.seg_log2), (h.ny + th_of(h.seg_log2) - 1) / th_of(h.seg_log2));
   if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_UNIFORM><<<grid, kThreads, 0, s>>>(h, stats);
+  else if (h.interp && h.compact)
+    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, stats);
   else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, stats);
   else if (h.axes_lut) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_LUT><<<grid, kThreads, 0, s>>>(h, stats);
   else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_UNIFORM><<<grid, kThreads, 0, s>>>(h, stats);
@@ -932,6 +995,8 @@ int persistent_grid(int cls) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (cls == BATCH_CUBE_TRI)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI>, kThreads, 0);
+  else if (cls == BATCH_CUBE_TRI_COMPACT)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI_COMPACT>, kThreads, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_ANY>, kThreads, 0);
   if (per_sm < 1) per_sm = 1;
@@ -940,6 +1005,7 @@ int persistent_grid(int cls) {
 
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int cls) {
   if (cls == BATCH_CUBE_TRI) render_batch_kernel<BATCH_CUBE_TRI><<<grid, kThreads, 0, s>>>(b);
+  else if (cls == BATCH_CUBE_TRI_COMPACT) render_batch_kernel<BATCH_CUBE_TRI_COMPACT><<<grid, kThreads, 0, s>>>(b);
   else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b);
   return cudaGetLastError();
 }

@@ -122,6 +122,7 @@ birp_status make_resident(birp_server* s, int id, std::unique_lock<std::mutex>& 
   }
   // upload outside the lock (the source is pinned by in_use)
   birp_cube* c = new birp_cube();
+  c->layout = s->cfg.cube_layout;
   birp_status rc = BIRP_OK;
   s->resident_bytes += src.bytes;
   const float* vals = src.h_vals;
@@ -297,6 +298,7 @@ void birp_server_default_config(birp_server_config* c) {
   c->max_batch_pixels = (int64_t)8 << 20;
   c->max_queue = 1 << 16;
   c->max_wait_ms = 1.0;
+  c->cube_layout = BIRP_CUBE_RECORDS;
 }
 
 birp_status birp_server_create(const birp_server_config* cfg, birp_server** out) {
@@ -307,7 +309,8 @@ birp_status birp_server_create(const birp_server_config* cfg, birp_server** out)
   birp_server_default_config(&c);
   if (cfg) c = *cfg;
   if (c.slots < 1 || c.slots > 16 || c.max_batch_requests < 1 || c.max_batch_pixels < 1 || c.max_queue < 1 ||
-      c.cube_budget_bytes < 0 || !(c.max_wait_ms >= 0))
+      c.cube_budget_bytes < 0 || !(c.max_wait_ms >= 0) ||
+      (c.cube_layout != BIRP_CUBE_RECORDS && c.cube_layout != BIRP_CUBE_COMPACT))
     return fail(BIRP_ERR_INVALID, "bad server configuration");
   birp_server* s = new birp_server();
   s->cfg = c;
@@ -384,6 +387,7 @@ birp_status birp_server_add_cube(birp_server* s, const double* xs, int nx, const
                                  const double* zs, int nz, const float* values, int* cube_id) {
   if (!s || !cube_id || !values || !xs || !ys || !zs) return fail(BIRP_ERR_INVALID, "NULL argument");
   birp_cube probe;
+  probe.layout = s->cfg.cube_layout;
   const double* axes[3] = {xs, ys, zs};
   const int n[3] = {nx, ny, nz};
   for (int k = 0; k < 3; ++k)

@@ -60,12 +60,24 @@ const char* birp_last_error(void);
  * never fires, src/Helper.cpp:616, so it treats every axis as uniform). */
 birp_status birp_cube_create(const double* xs, int nx, const double* ys, int ny, const double* zs, int nz,
                              const float* values, birp_cube** out);
+/* Device layouts of a cube (no reference counterpart: the reference keeps
+ * nested std::vectors on the host).
+ *   RECORDS: one 32-byte record of trilinear coefficients per cell, about 8x
+ *            the FP32 values; the fastest to render (the default).
+ *   COMPACT: the FP32 node values plus a guard layer, about 1x; the kernels
+ *            form each cell's coefficients from its 8 corners. For holding
+ *            many cubes under a memory budget (birp_server_config). */
+enum { BIRP_CUBE_RECORDS = 0, BIRP_CUBE_COMPACT = 1 };
+/* birp_cube_create with an explicit layout. */
+birp_status birp_cube_create_layout(const double* xs, int nx, const double* ys, int ny, const double* zs, int nz,
+                                    const float* values, int layout, birp_cube** out);
 birp_status birp_cube_destroy(birp_cube* cube);
 
 typedef struct {
   int nx, ny, nz;
   int uniform[3];          /* 1 where the axis is uniform (affine index) */
   size_t device_bytes;     /* GPU memory held by the cube */
+  int layout;              /* BIRP_CUBE_RECORDS or BIRP_CUBE_COMPACT */
 } birp_cube_info;
 birp_status birp_cube_get_info(const birp_cube* cube, birp_cube_info* info);
 
@@ -211,6 +223,7 @@ typedef struct {
   int64_t max_batch_pixels;
   int max_queue;               /* pending requests before submit returns BIRP_ERR_BUSY */
   double max_wait_ms;          /* batching window: launch when this old or the batch is full */
+  int cube_layout;             /* device layout of the server's cubes (BIRP_CUBE_*) */
 } birp_server_config;
 
 typedef struct {

@@ -1,0 +1,116 @@
+"""The compact cube layout (FP32 node values, coefficients formed per cell in
+the kernel) against the FP64 oracle and against the records layout, through
+the C ABI: plain renders, point samples, batches mixing both layouts, and a
+server holding its cubes compact.
+
+Tolerance: max relative error <= 1e-5 on pixels above 1e-3 of the image
+maximum; counts and nearest-node choices exact.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+THREADS = os.cpu_count() or 4
+
+
+@pytest.fixture(scope="module")
+def cubes(birp):
+    from birp_cpp_gb300 import synth
+    xs, ys, zs, v64 = synth.cube_config1(seed=1, n=128)
+    v32 = v64.astype(np.float32)
+    return dict(xs=xs, ys=ys, zs=zs, v32=v32, v64=v32.astype(np.float64),
+                rec=birp.Cube(xs, ys, zs, v32), cmp=birp.Cube(xs, ys, zs, v32, layout=birp.CUBE_COMPACT))
+
+
+def o_cam(oracle, cam):
+    return oracle.camera64(tuple(cam.pos), tuple(cam.aim), cam.fov_w_deg, cam.fov_h_deg, cam.nx, cam.ny,
+                           cam.n_samples, cam.ray_length, cam.march)
+
+
+def test_compact_memory_and_info(birp, cubes):
+    ir, ic = cubes["rec"].info(), cubes["cmp"].info()
+    assert ir.layout == birp.CUBE_RECORDS and ic.layout == birp.CUBE_COMPACT
+    nodes = 130 ** 3
+    assert nodes * 4 <= ic.device_bytes < nodes * 4 * 1.1
+    assert ir.device_bytes > 7 * ic.device_bytes
+
+
+def test_compact_constant_field_exact(birp, oracle):
+    from birp_cpp_gb300 import synth
+    xs, ys, zs = synth.stretched_axis(-40, 30, 64), synth.stretched_axis(-40, 40, 48), np.linspace(-40, 40, 33)
+    ones = np.ones((len(zs), len(ys), len(xs)))
+    g = birp.Cube(xs, ys, zs, ones.astype(np.float32), layout=birp.CUBE_COMPACT)
+    oc = oracle.Cube64(xs, ys, zs, ones, 1)
+    for pos, aim in [((1, 2, 3), (9, 0, 0)), ((-30, 25, -35), (4, 0, 0)), ((0.0, 0.0, 0.0), (9, 0, 0))]:
+        for march in (birp.PREFIX, birp.CLIP):
+            for tri in (True, False):
+                cam = birp.camera(pos, aim, 40.0, 30.0, 61, 37, n_samples=880, trilinear=tri, march=march)
+                img = birp.render(g, cam)
+                ref = oracle.render64(oc, o_cam(oracle, cam), threads=THREADS).astype(np.float32)
+                assert np.array_equal(img, ref), (pos, march, tri, int((img != ref).sum()))
+    g.close()
+
+
+@pytest.mark.parametrize("tri", [True, False])
+def test_compact_parity_vs_oracle(birp, oracle, cubes, tri):
+    from birp_cpp_gb300 import synth
+    oc = oracle.Cube64(cubes["xs"], cubes["ys"], cubes["zs"], cubes["v64"], int(tri))
+    for pos, aim, _, _, step in synth.config2_requests(5, seed=31):
+        cam = birp.camera(pos, aim, 27.0, 16.0, 96, 56, n_samples=synth.n_samples(step), trilinear=tri)
+        img = birp.render(cubes["cmp"], cam)
+        ref = oracle.render64(oc, o_cam(oracle, cam), threads=THREADS)
+        mx, rms, n = rel_err(img, ref)
+        assert mx <= TOL, (pos, tri, mx, rms)
+        # nearest mode reads the same node values in both layouts: same bits
+        if not tri:
+            assert np.array_equal(img, birp.render(cubes["rec"], cam))
+        else:
+            mx2, _, _ = rel_err(img, birp.render(cubes["rec"], cam))
+            assert mx2 <= 2 * TOL
+
+
+def test_compact_point_samples(birp, cubes):
+    rng = np.random.default_rng(8)
+    pts = rng.uniform(-45, 35, (4000, 3)).astype(np.float32)
+    for tri in (False, True):
+        a = cubes["cmp"].sample(pts, trilinear=tri)
+        b = cubes["rec"].sample(pts, trilinear=tri)
+        assert np.array_equal(a == -1, b == -1)
+        if tri:
+            assert np.allclose(a, b, rtol=1e-6, atol=1e-7)
+        else:
+            assert np.array_equal(a, b)
+
+
+def test_batch_mixing_layouts_equals_plain(birp, cubes):
+    from birp_cpp_gb300 import synth
+    items = []
+    for k, (pos, aim, nx, ny, step) in enumerate(synth.config2_requests(16, seed=33)):
+        cam = birp.camera(pos, aim, 27.0, 16.0, max(8, nx // 6), max(6, ny // 6), n_samples=synth.n_samples(step),
+                          trilinear=bool(k % 3), march=k % 2)
+        items.append((cubes["cmp"] if k % 2 else cubes["rec"], cam))
+    b = birp.Batch(32, 1 << 22)
+    outs = b.render(items)
+    for (sp, cam), img in zip(items, outs):
+        assert np.array_equal(img, birp.render(sp, cam))
+    b.close()
+
+
+def test_server_compact_cubes(birp, cubes):
+    srv = birp.Server(birp.server_config(cube_layout=birp.CUBE_COMPACT, cube_budget_bytes=1 << 30, slots=2))
+    cid = srv.add_cube(cubes["xs"], cubes["ys"], cubes["zs"], cubes["v32"])
+    cam = birp.camera((3, -9, 11), (9, 0, 0), 27.0, 16.0, 144, 84, n_samples=880)
+    out = np.empty((84, 144), np.float32)
+    t = srv.submit(cid, cam, out)
+    r = srv.wait(t, 60000)
+    assert r.status == 0
+    assert np.array_equal(out, birp.render(cubes["cmp"], cam))
+    st = srv.stats()
+    assert 0 < st.resident_bytes < 1.1 * 130 ** 3 * 4 + (1 << 20)
+    srv.close()
