@@ -1,9 +1,11 @@
 """Autotuner for the lanes-per-ray choice (S = 1, 2, 4, 8) of the render
 kernels. For each image-size class and sample-count class of the benchmark
-workloads it times plain renders of the 256^3 stretched cube from several
-orbit poses with every S (CUDA events around the kernel, L2 flushed before
-each) and writes the fastest choice per class to csrc/tune_table.inc (or the
-path given), which the library compiles in. Run on the GPU:
+workloads it times, with every S, (a) plain renders of the 256^3 stretched
+cube from several orbit poses and (b) batches of 32 such requests (CUDA
+events around the kernels, L2 flushed before each), and writes the fastest
+choice per class for a request rendered alone and for one inside a batch to
+csrc/tune_table.inc (or the path given), which the library compiles in. Run
+on the GPU:
 
     python -m birp_cpp_gb300.autotune --out birp_cpp_gb300/csrc/tune_table.inc
 """
@@ -57,28 +59,66 @@ def tune(n_poses: int = 4, repeats: int = 3, kind: str = "cube"):
                 if best is None or times[s] < times[best]:
                     best = s
             results[(nx * ny, n)] = (best, times)
-            print(json.dumps({"pixels": nx * ny, "n_samples": n, "best": best,
+            print(json.dumps({"context": "plain", "pixels": nx * ny, "n_samples": n, "best": best,
                               "ms": {str(k): round(v, 4) for k, v in times.items()}}), flush=True)
     return results
 
 
-def write_table(results, path, kind_code=-1):
+def tune_batch(batch_size: int = 32, repeats: int = 3):
+    """Kernel time of a batch of `batch_size` requests of one class (orbit
+    poses) for every S; returns {(pixels, samples): (best S, times)}."""
+    import birp_cpp_gb300 as B
+    from birp_cpp_gb300 import build, synth
+    build.build()
+    B.init(0)
+    xs, ys, zs, v = synth.cube_config1(seed=1)
+    cube = B.Cube(xs, ys, zs, v.astype(np.float32))
+    poses = [(p, a) for p, a, *_ in synth.config2_requests(batch_size, seed=78)]
+    batch = B.Batch(batch_size, batch_size * 1024 * 600)
+    results = {}
+    for nx, ny in SIZES:
+        for n in SAMPLES:
+            times = {}
+            for s in SEGMENTS:
+                items = [(cube, B.camera(p, a, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=n, segments=s))
+                         for p, a in poses]
+                ms = []
+                for _ in range(repeats):
+                    B.flush_l2()
+                    batch.submit(items)
+                    batch.wait()
+                    ms.append(batch.last_ms()[0])
+                times[s] = float(np.median(ms))
+            best = min(times, key=times.get)
+            results[(nx * ny, n)] = (best, times)
+            print(json.dumps({"context": "batch", "pixels": nx * ny, "n_samples": n, "best": best,
+                              "ms": {str(k): round(v, 4) for k, v in times.items()}}), flush=True)
+    return results
+
+
+def _rows(results, kind_code=-1):
     """Rows ordered by pixels then samples; each row covers pixels up to its
     class (and the geometric midpoint to the next class)."""
     pix = sorted({p for p, _ in results})
     smp = sorted({n for _, n in results})
-    lines = ["// Lanes-per-ray table: the first row whose bounds hold gives log2(lanes).",
-             "// kind: 0 cube, 1 CMEM, -1 any; trilinear: -1 any.",
-             "// Written by birp_cpp_gb300/autotune.py from plain-render timings on a GB300",
-             "// (256^3 stretched cube, orbit poses, L2 flushed before each render).",
-             "static const TuneRow kTuneRows[] = {"]
+    out = []
     for i, p in enumerate(pix):
         pmax = int(np.sqrt(p * pix[i + 1])) if i + 1 < len(pix) else (1 << 40)
         for j, n in enumerate(smp):
             nmax = int(np.sqrt(n * smp[j + 1])) if j + 1 < len(smp) else (1 << 30)
             best = results[(p, n)][0]
-            lines.append(f"    {{(int64_t){pmax}, {nmax}, {kind_code}, -1, {int(np.log2(best))}}},")
-    lines.append("};")
+            out.append(f"    {{(int64_t){pmax}, {nmax}, {kind_code}, -1, {int(np.log2(best))}}},")
+    return out
+
+
+def write_table(plain, batch, path):
+    lines = ["// Lanes-per-ray tables: the first row whose bounds hold gives log2(lanes).",
+             "// Columns: max pixels, max samples, kind (0 cube, 1 CMEM, -1 any), trilinear",
+             "// (-1 any), log2(lanes). Written by birp_cpp_gb300/autotune.py from timings on",
+             "// a GB300 (256^3 stretched cube, orbit poses, L2 flushed before each launch):",
+             "// plain renders for a request alone, 32-request batches for one in a batch.",
+             "static const TuneRow kTuneRowsPlain[] = {"] + _rows(plain) + ["};",
+             "static const TuneRow kTuneRowsBatch[] = {"] + _rows(batch) + ["};"]
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
 
@@ -89,8 +129,9 @@ def main():
     ap.add_argument("--poses", type=int, default=4)
     ap.add_argument("--repeats", type=int, default=3)
     args = ap.parse_args()
-    res = tune(args.poses, args.repeats)
-    write_table(res, args.out)
+    plain = tune(args.poses, args.repeats)
+    batch = tune_batch(repeats=args.repeats)
+    write_table(plain, batch, args.out)
     print("wrote", args.out)
 
 

@@ -130,7 +130,7 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* 
     b->offsets[i] = used;
     b->npx[i] = npx;
     float* out = direct_outs ? direct_outs[i] : b->d_out + used;
-    if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, out, rq[i])) return s;
+    if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, c, out, rq[i], true)) return s;
     used += npx;
     work[i] = (double)npx * c.n_samples * (reqs[i].cmem ? 16.0 : 1.0);
     members[request_class(reqs[i])].push_back(i);

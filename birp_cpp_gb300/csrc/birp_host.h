@@ -75,8 +75,9 @@ birp_status ok();
 birp_status check_init();
 birp_status validate_camera(const birp_camera* c);
 birp_status camera_frame(const birp_camera& c, Frame& f);
+// batched: the request is rendered inside a batch (lanes-per-ray table)
 birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const birp_camera& c, float* out,
-                          RequestDev& r);
+                          RequestDev& r, bool batched = false);
 cudaStream_t pick_stream(void* s);
 
 // cube.cu
@@ -92,6 +93,6 @@ birp_status ensure_xyz_scratch(size_t floats);
 void cmem_coefficients(const birp_cmem_params& p, CmemDev& m);
 
 // tune.cpp: lanes-per-ray choice from the committed tuning table
-int tuned_seg_log2(int64_t pixels, int n_samples, int kind, int trilinear);
+int tuned_seg_log2(int64_t pixels, int n_samples, int kind, int trilinear, bool batched);
 
 }  // namespace birp

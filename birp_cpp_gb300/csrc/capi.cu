@@ -181,18 +181,18 @@ birp_status validate_camera(const birp_camera* c) {
   return BIRP_OK;
 }
 
-// Lanes per ray: explicit, else the tuned table (birp_tune.cpp).
-int choose_seg_log2(const birp_camera& c, int kind) {
+// Lanes per ray: explicit, else the tuned tables (tune.cpp).
+int choose_seg_log2(const birp_camera& c, int kind, bool batched) {
   if (c.segments > 0) {
     int l = 0;
     while ((1 << l) < c.segments) ++l;
     return l;
   }
-  return tuned_seg_log2((int64_t)c.nx * c.ny, c.n_samples, kind, c.trilinear);
+  return tuned_seg_log2((int64_t)c.nx * c.ny, c.n_samples, kind, c.trilinear, batched);
 }
 
 birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const birp_camera& c, float* out,
-                          RequestDev& r) {
+                          RequestDev& r, bool batched) {
   birp_status st = validate_camera(&c);
   if (st) return st;
   if ((cube == nullptr) == (cmem == nullptr)) return fail(BIRP_ERR_INVALID, "exactly one of cube / cmem must be given");
@@ -218,7 +218,7 @@ birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const bi
   r.mode = c.march;
   r.interp = c.trilinear ? 1 : 0;
   r.kind = cube ? SPACE_CUBE : SPACE_CMEM;
-  r.seg_log2 = choose_seg_log2(c, r.kind);
+  r.seg_log2 = choose_seg_log2(c, r.kind, batched);
   r.tiles_x = (c.nx + tile_w(r.seg_log2) - 1) / tile_w(r.seg_log2);
   int tiles_y = (c.ny + tile_h(r.seg_log2) - 1) / tile_h(r.seg_log2);
   r.tiles = r.tiles_x * tiles_y;
@@ -653,15 +653,19 @@ birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs) {
   cudaStream_t st = g_ctx.stream;
   float* sink = nullptr;
   float4* buf = nullptr;
-  const size_t bytes = (size_t)48 << 20;  // well inside one die's half of L2
+  // L2 read rate: the largest over L2-resident buffers of 8, 16 and 32 MB
+  // (where a buffer's lines sit in the two dies' L2 halves varies with the
+  // allocation), each launch reading about 2 GB, best of 3 launches per size
+  const size_t max_bytes = (size_t)32 << 20;
   CK(cudaMalloc(&sink, sizeof(float)));
-  CK(cudaMalloc(&buf, bytes));
-  CK(cudaMemsetAsync(buf, 0, bytes, st));
+  CK(cudaMalloc(&buf, max_bytes));
+  CK(cudaMemsetAsync(buf, 0, max_bytes, st));
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  const int blocks = g_ctx.sms * 8, iters = 20000, reps = 20;
-  float best_f = 1e30f, best_r = 1e30f;
+  const int blocks = g_ctx.sms * 8, iters = 20000;
+  float best_f = 1e30f;
+  double best_gbs = 0.0;
   for (int rep = 0; rep < 3; ++rep) {
     float ms;
     CK(cudaEventRecord(e0, st));
@@ -670,19 +674,26 @@ birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs) {
     CK(cudaEventSynchronize(e1));
     CK(cudaEventElapsedTime(&ms, e0, e1));
     best_f = std::min(best_f, ms);
-    CK(cudaEventRecord(e0, st));
-    CK(launch_peak_read(buf, bytes / 16, reps, sink, g_ctx.sms * 4, st));
-    CK(cudaEventRecord(e1, st));
-    CK(cudaEventSynchronize(e1));
-    CK(cudaEventElapsedTime(&ms, e0, e1));
-    best_r = std::min(best_r, ms);
+  }
+  for (size_t bytes : {(size_t)8 << 20, (size_t)16 << 20, max_bytes}) {
+    const int reps = (int)(((size_t)2 << 30) / bytes);
+    CK(launch_peak_read(buf, bytes / 16, 1, sink, g_ctx.sms * 4, st));  // bring the buffer into L2
+    for (int rep = 0; rep < 3; ++rep) {
+      float ms;
+      CK(cudaEventRecord(e0, st));
+      CK(launch_peak_read(buf, bytes / 16, reps, sink, g_ctx.sms * 4, st));
+      CK(cudaEventRecord(e1, st));
+      CK(cudaEventSynchronize(e1));
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      best_gbs = std::max(best_gbs, (double)bytes * reps / (ms * 1e-3) / 1e9);
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(sink);
   cudaFree(buf);
   if (fp32_tflops) *fp32_tflops = 2.0 * 8 * iters * (double)blocks * 256 / (best_f * 1e-3) / 1e12;
-  if (l2_read_gbs) *l2_read_gbs = (double)bytes * reps / (best_r * 1e-3) / 1e9;
+  if (l2_read_gbs) *l2_read_gbs = best_gbs;
   return ok();
 }
 

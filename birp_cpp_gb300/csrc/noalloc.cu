@@ -86,7 +86,8 @@ extern "C" birp_status birp_batch_render_noalloc(const birp_request* reqs, int n
   int cls = n > 0 ? request_class(reqs[0]) : BATCH_ANY;
   for (int i = 0; i < n; ++i) {
     if (!outs_device[i]) return fail(BIRP_ERR_INVALID, "output %d is NULL", i);
-    if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, reqs[i].cam, outs_device[i], rq[i])) return s;
+    if (birp_status s = build_request(reqs[i].cube, reqs[i].cmem, reqs[i].cam, outs_device[i], rq[i], true))
+      return s;
     if (request_class(reqs[i]) != cls) cls = BATCH_ANY;
   }
   // largest work first (as the allocating batch path)

@@ -1,4 +1,6 @@
-// Lanes-per-ray choice from the committed tuning table (tune_table.inc).
+// Lanes-per-ray choice from the committed tuning tables (tune_table.inc): one
+// for a request rendered alone, one for a request inside a batch (where other
+// requests already fill the GPU).
 #include <cstdint>
 
 #include "birp_host.h"
@@ -15,8 +17,11 @@ struct TuneRow {
 
 #include "tune_table.inc"
 
-int tuned_seg_log2(int64_t pixels, int n_samples, int kind, int trilinear) {
-  for (const TuneRow& r : kTuneRows) {
+int tuned_seg_log2(int64_t pixels, int n_samples, int kind, int trilinear, bool batched) {
+  const TuneRow* rows = batched ? kTuneRowsBatch : kTuneRowsPlain;
+  const size_t n = batched ? sizeof(kTuneRowsBatch) / sizeof(TuneRow) : sizeof(kTuneRowsPlain) / sizeof(TuneRow);
+  for (size_t i = 0; i < n; ++i) {
+    const TuneRow& r = rows[i];
     if (pixels > r.max_pixels || n_samples > r.max_samples) continue;
     if (r.kind >= 0 && r.kind != kind) continue;
     if (r.trilinear >= 0 && r.trilinear != (trilinear ? 1 : 0)) continue;

@@ -29,7 +29,9 @@ def mixed_items(birp, spaces, n=24, seed=9):
         nx, ny = max(8, nx // 8), max(6, ny // 8)
         kind = rng.integers(0, 4)
         space = [spaces["c1"], spaces["c1"], spaces["c0"], spaces["cmem"]][kind]
-        cam = birp.camera(pos, aim, 27.0, 16.0, nx, ny, n_samples=synth.n_samples(step),
+        # explicit lanes per ray: a batch and a plain render then sum each
+        # ray in the same order (automatic choices differ between the two)
+        cam = birp.camera(pos, aim, 27.0, 16.0, nx, ny, n_samples=synth.n_samples(step), segments=2 ** (k % 4),
                           trilinear=bool(rng.integers(0, 2)), march=int(rng.integers(0, 2)))
         items.append((space, cam))
     return items
@@ -52,9 +54,27 @@ def test_batch_equals_plain_bitwise(birp, spaces):
     b.close()
 
 
+def test_batch_auto_lanes_close_to_plain(birp, spaces):
+    """With automatic lanes per ray a batch may split rays differently from a
+    plain render (its own tuned table); the images then differ only by FP32
+    summation order."""
+    from conftest import rel_err
+    items = [(sp, birp.camera(tuple(c.pos), tuple(c.aim), c.fov_w_deg, c.fov_h_deg, c.nx, c.ny,
+                              n_samples=c.n_samples, trilinear=bool(c.trilinear), march=c.march))
+             for sp, c in mixed_items(birp, spaces, n=16, seed=17)]
+    b = birp.Batch(32, 1 << 22)
+    for (sp, cam), img in zip(items, b.render(items)):
+        ref = birp.render(sp, cam)
+        if ref.max() > 0:
+            mx, _, _ = rel_err(img, ref.astype(np.float64))
+            assert mx <= 1e-5, mx  # the parity tolerance; both paths sit within it of the oracle
+        assert np.array_equal(img == 0, ref == 0)
+    b.close()
+
+
 def test_batch_single_and_empty(birp, spaces):
     b = birp.Batch(4, 1 << 16)
-    cam = birp.camera((3, 1, 2), (9, 0, 0), 27.0, 16.0, 40, 24, n_samples=440)
+    cam = birp.camera((3, 1, 2), (9, 0, 0), 27.0, 16.0, 40, 24, n_samples=440, segments=2)
     [img] = b.render([(spaces["c1"], cam)])
     assert np.array_equal(img, birp.render(spaces["c1"], cam))
     assert b.render([]) == []
@@ -134,7 +154,7 @@ def test_server_lru_eviction_and_errors(birp, spaces):
                                          max_batch_pixels=1 << 18, max_wait_ms=0.0))
     ids = [srv.add_cube(*c) for c in cubes]
     gpu_cubes = [birp.Cube(*c) for c in cubes]
-    cam = birp.camera((2, -3, 4), (9, 0, 0), 27.0, 16.0, 48, 28, n_samples=440)
+    cam = birp.camera((2, -3, 4), (9, 0, 0), 27.0, 16.0, 48, 28, n_samples=440, segments=1)
     for rnd in range(3):
         for k in (0, 1, 2):
             o = np.empty((28, 48), np.float32)

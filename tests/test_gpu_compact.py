@@ -93,7 +93,7 @@ def test_batch_mixing_layouts_equals_plain(birp, cubes):
     items = []
     for k, (pos, aim, nx, ny, step) in enumerate(synth.config2_requests(16, seed=33)):
         cam = birp.camera(pos, aim, 27.0, 16.0, max(8, nx // 6), max(6, ny // 6), n_samples=synth.n_samples(step),
-                          trilinear=bool(k % 3), march=k % 2)
+                          trilinear=bool(k % 3), march=k % 2, segments=2 ** (k % 4))
         items.append((cubes["cmp"] if k % 2 else cubes["rec"], cam))
     b = birp.Batch(32, 1 << 22)
     outs = b.render(items)
@@ -105,7 +105,7 @@ def test_batch_mixing_layouts_equals_plain(birp, cubes):
 def test_server_compact_cubes(birp, cubes):
     srv = birp.Server(birp.server_config(cube_layout=birp.CUBE_COMPACT, cube_budget_bytes=1 << 30, slots=2))
     cid = srv.add_cube(cubes["xs"], cubes["ys"], cubes["zs"], cubes["v32"])
-    cam = birp.camera((3, -9, 11), (9, 0, 0), 27.0, 16.0, 144, 84, n_samples=880)
+    cam = birp.camera((3, -9, 11), (9, 0, 0), 27.0, 16.0, 144, 84, n_samples=880, segments=1)
     out = np.empty((84, 144), np.float32)
     t = srv.submit(cid, cam, out)
     r = srv.wait(t, 60000)
