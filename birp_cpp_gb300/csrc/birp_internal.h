@@ -136,9 +136,15 @@ cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaS
 // Persistent batch kernel classes: CUBE_TRI renders only trilinear cube
 // requests (fewer registers, more resident warps); ANY renders every kind.
 // Persistent-kernel classes of a batch: trilinear cube requests in the
-// records layout, the same in the compact layout, and everything else (CMEM,
-// nearest mode) in the general kernel.
-enum BatchClass : int { BATCH_CUBE_TRI = 0, BATCH_ANY = 1, BATCH_CUBE_TRI_COMPACT = 2, BATCH_CLASSES = 3 };
+// records layout, the same in the compact layout, CMEM requests, and
+// everything else (nearest mode) in the general kernel.
+enum BatchClass : int {
+  BATCH_CUBE_TRI = 0,
+  BATCH_ANY = 1,
+  BATCH_CUBE_TRI_COMPACT = 2,
+  BATCH_CMEM = 3,
+  BATCH_CLASSES = 4
+};
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);

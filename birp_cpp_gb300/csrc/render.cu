@@ -34,6 +34,9 @@ namespace birp {
 namespace {
 
 constexpr int kThreads = 128;
+#ifndef BIRP_CMEM_MINB
+#define BIRP_CMEM_MINB 6  // resident CTAs per SM the CMEM batch kernel is compiled for
+#endif
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 // Bound on |d32 - d64| per component of the unit ray direction. d32 is the
@@ -94,7 +97,7 @@ __device__ __forceinline__ double pos64(double p, double d, double dt, int i) {
 
 // Exact FP64 unit direction of the ray from w = A_i + B_j (the FP64 oracle's
 // normalize(R^-1 (sx, sy, -1))).
-__device__ void dir64(const double* w, double* d) {
+__device__ __noinline__ void dir64(const double* w, double* d) {
   double n2 = __dadd_rn(__dadd_rn(__dmul_rn(w[0], w[0]), __dmul_rn(w[1], w[1])), __dmul_rn(w[2], w[2]));
   double inv = __ddiv_rn(1.0, __dsqrt_rn(n2));
   d[0] = __dmul_rn(w[0], inv);
@@ -189,61 +192,94 @@ struct CmemEval {
 
 // CMEM::GetSample in FP32 (src/Cmem.cpp:117-186 with ShueCoords :224-246,
 // LinScaled :188-222, ShueModel :280-288), rewritten in forms that stay
-// well conditioned in FP32 (the same values in exact arithmetic):
-//   theta = acos(x/r)           -> atan2(sqrt(y^2+z^2), x)
-//   phi   = acos(y/sqrt(y^2+z^2)) -> atan2(|z|, y)
-//   phi_n = acos(u . n_N)       -> atan2(|u x n_N|, u . n_N), with the unit
+// well conditioned in FP32 and avoid most transcendental calls (the same
+// values in exact arithmetic):
+//   cos t, sin t = x / r, r_yz / r; cos p, sin p = y / r_yz, |z| / r_yz
+//   theta       = acos(x/r)       -> atan2(r_yz, x)   (needed itself: exp(-t), t^4)
+//   2 / (1 + cos t)               -> 2r / (r + x) for x >= 0, else 2r (r - x) / r_yz^2
+//   cos(t/2)                      -> sqrt((1 + cos t) / 2)
+//   phi_n = acos(u . n_N)         -> atan2(|u x n_N|, u . n_N), with the unit
 //           direction u = (cos t, sin t cos p, sin t sin p) and the cusp axis
 //           n_N = (cos t_n, 0, sin t_n) (cos(p - pi/2) = sin p); n_S likewise
 //           with -sin t_s (cos(p - 3pi/2) = -sin p)
-//   2 / (1 + cos t)             -> 1 / cos^2(t/2)
+//   a^b, exp(a)                   -> exp2(b log2 a), exp2(a log2 e); the two
+//           bow-shock powers of 2/(1 + cos t) share one log2
 // and the reference's quirks kept: theta = 0 when x == 0, phi = 0 when y == 0.
 // `unsure` flags samples whose shell choice lies within the FP32 error bound
 // (eps_rel * (r + 5 Re): relative with an absolute floor for the small radii
 // where the Lin model cancels, plus the position error perr) of a
-// discontinuous edge.
-__device__ __forceinline__ void cmem_angles32(float x, float y, float z, float& r, float& theta, float& phi) {
-  float ryz = sqrtf(y * y + z * z);
-  r = sqrtf(x * x + y * y + z * z);
-  theta = (x != 0.f) ? atan2f(ryz, x) : 0.f;
-  phi = (y != 0.f) ? atan2f(fabsf(z), y) : 0.f;
+// discontinuous edge; the bound is checked on the GPU by
+// birp_cmem_margin_check.
+struct CmemDir {
+  float r, theta, ct, st, cp, sp, b2;  // b2 = 2 / (1 + cos theta)
+};
+
+__device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
+  CmemDir d;
+  const float ryz2 = fmaf(y, y, z * z);
+  const float ryz = sqrtf(ryz2);
+  d.r = sqrtf(fmaf(x, x, ryz2));
+  if (x != 0.f) {
+    d.theta = atan2f(ryz, x);
+    const float ir = 1.f / d.r;
+    d.ct = x * ir;
+    d.st = ryz * ir;
+    d.b2 = x >= 0.f ? 2.f * d.r / (d.r + x) : 2.f * d.r * (d.r - x) / ryz2;
+  } else {
+    d.theta = 0.f;
+    d.ct = 1.f;
+    d.st = 0.f;
+    d.b2 = 1.f;
+  }
+  if (y != 0.f) {
+    const float iyz = 1.f / ryz;
+    d.cp = y * iyz;
+    d.sp = fabsf(z) * iyz;
+  } else {
+    d.cp = 1.f;
+    d.sp = 0.f;
+  }
+  return d;
 }
 
-__device__ __forceinline__ void cmem_radii32(const CmemDev& m, float theta, float phi, float& r_mp, float& r_bs,
-                                             float& st, float& ct, float& sp, float& cp) {
-  sincosf(theta, &st, &ct);
-  sincosf(phi, &sp, &cp);
+__device__ __forceinline__ float pow_pos(float a, float b) { return exp2f(b * __log2f(a)); }
+
+constexpr float kLog2e = 1.4426950408889634f;
+
+__device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d, float& r_mp, float& r_bs) {
   // angle to the northern / southern cusp axes
-  const float ux = ct, uy = st * cp, uz = st * sp;
+  const float ux = d.ct, uy = d.st * d.cp, uz = d.st * d.sp;
   float dn = ux * m.cos_tn + uz * m.sin_tn;
   float cnx = uy * m.sin_tn, cny = uz * m.cos_tn - ux * m.sin_tn, cnz = -uy * m.cos_tn;
   float phi_n = atan2f(sqrtf(cnx * cnx + cny * cny + cnz * cnz), dn);
   float ds = ux * m.cos_ts - uz * m.sin_ts;
   float csx = -uy * m.sin_ts, csy = uz * m.cos_ts + ux * m.sin_ts, csz = -uy * m.cos_ts;
   float phi_s = atan2f(sqrtf(csx * csx + csy * csy + csz * csz), ds);
-  float ch = cosf(0.5f * theta);
-  float base = ch + m.a5 * (2.f * st * ct) * (1.f - expf(-theta));
-  float f = powf(base, m.p1 * (m.bc0 + m.bc1 * cp + m.bc3 * (sp * sp)));
-  float q = m.p2c * expf(m.p3dn * powf(phi_n, m.a21)) + m.p2c * expf(m.p3ds * powf(phi_s, m.a21));
+  const float ch = sqrtf(1.f / d.b2);  // cos(theta / 2)
+  float base = ch + m.a5 * (2.f * d.st * d.ct) * (1.f - exp2f(-kLog2e * d.theta));
+  float f = pow_pos(base, m.p1 * (m.bc0 + m.bc1 * d.cp + m.bc3 * (d.sp * d.sp)));
+  float q = m.p2c * exp2f(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
+            m.p2c * exp2f(kLog2e * m.p3ds * pow_pos(phi_s, m.a21));
   r_mp = m.p0r0 * f + q;
-  float b2 = 1.f / (ch * ch);
-  float ry = m.bs * powf(b2, m.ay);
-  float rz = m.bs * powf(b2, m.az);
-  float a1 = rz * cp, a2 = ry * sp;
+  const float lb = __log2f(d.b2);
+  float ry = m.bs * exp2f(m.ay * lb);
+  float rz = m.bs * exp2f(m.az * lb);
+  float a1 = rz * d.cp, a2 = ry * d.sp;
   r_bs = (ry * rz) / sqrtf(a1 * a1 + a2 * a2);
 }
 
 __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
-  float r, theta, phi, r_mp, r_bs, st, ct, sp, cp;
-  cmem_angles32(x, y, z, r, theta, phi);
-  cmem_radii32(m, theta, phi, r_mp, r_bs, st, ct, sp, cp);
+  const CmemDir d = cmem_dir32(x, y, z);
+  float r_mp, r_bs;
+  cmem_radii32(m, d, r_mp, r_bs);
+  const float r = d.r;
   const float half = 0.025f;
   CmemEval out;
   float tol = fmaf(m.eps_rel, r + 5.f, perr);
   out.unsure = !(fabsf(r - (r_mp + half)) > tol) || !(fabsf(r - (r_bs + half)) > tol);
-  float h = 0.5f * theta;
+  float h = 0.5f * d.theta;
   float h4 = (h * h) * (h * h);
-  float sheath = m.A1 * expf(-m.B * h4) * powf(r * 0.1f, -m.alpha - m.beta * (st * st));
+  float sheath = m.A1 * exp2f(-kLog2e * m.B * h4) * pow_pos(r * 0.1f, -m.alpha - m.beta * (d.st * d.st));
   float d10 = r * 0.1f;
   float outer = m.A2 / (d10 * d10 * d10);
   float v;
@@ -257,7 +293,9 @@ __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, floa
 }
 
 // The same in FP64 with the FP64 oracle's formulas (oracle cmem64_sample).
-__device__ double cmem_value64(const CmemDev& m, double x, double y, double z) {
+// (not inlined: the fallback is rare, and inlining it would raise the
+// register count of every loop that may call it)
+__device__ __noinline__ double cmem_value64(const CmemDev& m, double x, double y, double z) {
   const double pi = 3.14159265358979323846;
   double r = sqrt(x * x + y * y + z * z);
   double theta = (x != 0) ? acos(x / r) : 0.0;
@@ -736,7 +774,8 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
 // first). CLS = BATCH_CUBE_TRI compiles only the trilinear cube march (fewer
 // registers, more resident warps); BATCH_ANY renders every request kind.
 template <int CLS>
-__global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY ? 1 : 8) render_batch_kernel(BatchDev B) {
+__global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY ? 1 : CLS == BATCH_CMEM ? BIRP_CMEM_MINB : 8)
+    render_batch_kernel(BatchDev B) {
   __shared__ TileSmem sm;
   __shared__ int s_item;
   const int n_reqs = __ldg(B.hdr), total_items = __ldg(B.hdr + 1);
@@ -761,6 +800,8 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY ? 1 : 8) render_bat
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CUBE_TRI_COMPACT) {
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
+    } else if constexpr (CLS == BATCH_CMEM) {
+      render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM>(R, tx, ty, sm, B.stats);
     } else {
       render_tile_any(R, tx, ty, sm, B.stats);
     }
@@ -913,11 +954,17 @@ __global__ void cmem_radii_check_kernel(const CmemDev* __restrict__ cmem, int n,
     h ^= h >> 29;
     h *= 0xBF58476D1CE4E5B9ull;
     h ^= h >> 32;
-    float theta = (float)((h & 0xFFFFFF) * (pi * 0.999 / 16777216.0));
-    float phi = (float)(((h >> 24) & 0xFFFFFF) * (pi / 16777216.0));
-    float r_mp, r_bs, st32, ct32, sp32, cp32;
-    cmem_radii32(m, theta, phi, r_mp, r_bs, st32, ct32, sp32, cp32);
-    double th = theta, ph = phi;
+    // an FP32 point at 10 Re in a pseudo-random direction; both radii are
+    // computed from that same point (FP32 path vs FP64 with the oracle's
+    // acos forms)
+    const double th0 = (h & 0xFFFFFF) * (pi * 0.999 / 16777216.0);
+    const double ph0 = ((h >> 24) & 0xFFFFFF) * (pi / 16777216.0);
+    const float x = (float)(10.0 * cos(th0)), y = (float)(10.0 * sin(th0) * cos(ph0)),
+                z = (float)(10.0 * sin(th0) * sin(ph0));
+    float r_mp, r_bs;
+    cmem_radii32(m, cmem_dir32(x, y, z), r_mp, r_bs);
+    const double X = x, Y = y, Z = z, R = sqrt(X * X + Y * Y + Z * Z);
+    double th = (X != 0) ? acos(X / R) : 0.0, ph = (Y != 0) ? acos(Y / sqrt(Y * Y + Z * Z)) : 0.0;
     double phi_n = acos(cos(th) * cos(m.d_tn) + sin(th) * sin(m.d_tn) * cos(ph - pi / 2));
     double phi_s = acos(cos(th) * cos(m.d_ts) + sin(th) * sin(m.d_ts) * cos(ph - 3 * pi / 2));
     double sp = sin(ph);
@@ -997,6 +1044,8 @@ int persistent_grid(int cls) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI>, kThreads, 0);
   else if (cls == BATCH_CUBE_TRI_COMPACT)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI_COMPACT>, kThreads, 0);
+  else if (cls == BATCH_CMEM)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CMEM>, kThreads, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_ANY>, kThreads, 0);
   if (per_sm < 1) per_sm = 1;
@@ -1006,6 +1055,7 @@ int persistent_grid(int cls) {
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int cls) {
   if (cls == BATCH_CUBE_TRI) render_batch_kernel<BATCH_CUBE_TRI><<<grid, kThreads, 0, s>>>(b);
   else if (cls == BATCH_CUBE_TRI_COMPACT) render_batch_kernel<BATCH_CUBE_TRI_COMPACT><<<grid, kThreads, 0, s>>>(b);
+  else if (cls == BATCH_CMEM) render_batch_kernel<BATCH_CMEM><<<grid, kThreads, 0, s>>>(b);
   else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b);
   return cudaGetLastError();
 }
