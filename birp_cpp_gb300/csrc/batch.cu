@@ -24,7 +24,7 @@ static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 int request_class(const birp_request& r) {
   if (r.cmem) return BATCH_CMEM;
-  if (!r.cam.trilinear) return BATCH_ANY;
+  if (!r.cam.trilinear) return BATCH_CUBE_NEAREST;
   return (r.cube && r.cube->layout == BIRP_CUBE_COMPACT) ? BATCH_CUBE_TRI_COMPACT : BATCH_CUBE_TRI;
 }
 
@@ -82,10 +82,11 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   std::memset(b->h_stage, 0, b->stage_bytes);
 
   // One graph: descriptors H2D, the queue heads reset, then the CMEM kernel
-  // and the general kernel (nearest mode; few but heavy requests, so they
-  // start first) and the two trilinear-cube kernels (compact, then records
-  // layout; 64 registers, full occupancy). A class with no requests costs one
-  // launch whose CTAs exit at once.
+  // (few but heavy requests, so they start first), the nearest-mode kernel
+  // and the two trilinear-cube kernels (compact, then records layout; 64
+  // registers, full occupancy). A class with no requests costs one launch
+  // whose CTAs exit at once; every request falls in one of these classes, so
+  // the general kernel is not launched.
   BatchDev bd[BATCH_CLASSES];
   for (int c = 0; c < BATCH_CLASSES; ++c) {
     bd[c].hdr = reinterpret_cast<const int*>(b->d_stage) + 4 * c;
@@ -100,7 +101,7 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
     return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
   cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
   cudaMemsetAsync(b->d_counter, 0, BATCH_CLASSES * sizeof(unsigned int), b->stream);
-  for (int c : {BATCH_CMEM, BATCH_ANY, BATCH_CUBE_TRI_COMPACT, BATCH_CUBE_TRI})
+  for (int c : {BATCH_CMEM, BATCH_CUBE_NEAREST, BATCH_CUBE_TRI_COMPACT, BATCH_CUBE_TRI})
     launch_render_batch(bd[c], b->grid[c], b->stream, c);
   e = cudaStreamEndCapture(b->stream, &b->graph);
   if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));

@@ -25,6 +25,7 @@ struct birp_cube {
   int layout = BIRP_CUBE_RECORDS;
   float* d_grid = nullptr;      // compact layout: padded node values
   float4* d_walk4 = nullptr;    // compact layout: walk tables with inverse widths
+  float2* d_nodes_ff = nullptr; // node coordinates as float pairs, 3 axes concatenated
   size_t device_bytes = 0;
   cudaStream_t alloc_stream = nullptr;  // non-null: stream-ordered (pool) allocations
 };

@@ -60,6 +60,10 @@ struct CubeDev {
   // entries, j in [-1, n-1]
   const float2* walk_up[3];
   const float2* walk_dn[3];
+  // node coordinates of each axis as float pairs {hi, lo} (hi + lo = the
+  // FP64 coordinate to ~48 bits), for the nearest-mode crossings; entries
+  // -1 and n are the sentinels -inf and +inf
+  const float2* nodes_ff[3];
   // compact layout (rec == nullptr): padded node values and their strides,
   // and the float4 walk tables (same indexing as walk_up / walk_dn)
   int compact;
@@ -92,6 +96,10 @@ struct RequestDev {
   double K;          // per-sample scale (src/Camera.cpp:201 with ray_width = dt)
   float pos32[3];
   float dt32;
+  // pos and dt as float pairs (hi + lo, ~48-bit significands): the nearest-mode
+  // walk computes its cell crossings in this float-float arithmetic
+  float pos_hi[3], pos_lo[3];
+  float dt_hi, dt_lo;
   int nx, ny, N;
   int mode;          // MarchMode
   int interp;        // 1 trilinear, 0 nearest
@@ -135,15 +143,17 @@ struct BatchDev {
 cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaStream_t stream);
 // Persistent batch kernel classes: CUBE_TRI renders only trilinear cube
 // requests (fewer registers, more resident warps); ANY renders every kind.
-// Persistent-kernel classes of a batch: trilinear cube requests in the
-// records layout, the same in the compact layout, CMEM requests, and
-// everything else (nearest mode) in the general kernel.
+// Persistent-kernel classes: trilinear cube requests in the records layout,
+// the same in the compact layout, CMEM requests, nearest-mode cube requests
+// (either layout), and the general kernel that renders any request (used
+// where one launch must take a mix, see birp_batch_render_noalloc).
 enum BatchClass : int {
   BATCH_CUBE_TRI = 0,
   BATCH_ANY = 1,
   BATCH_CUBE_TRI_COMPACT = 2,
   BATCH_CMEM = 3,
-  BATCH_CLASSES = 4
+  BATCH_CUBE_NEAREST = 4,
+  BATCH_CLASSES = 5
 };
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
 int persistent_grid(int cls);

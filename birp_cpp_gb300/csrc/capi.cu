@@ -208,9 +208,13 @@ birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const bi
   for (int k = 0; k < 3; ++k) {
     r.pos[k] = c.pos[k];
     r.pos32[k] = (float)c.pos[k];
+    r.pos_hi[k] = r.pos32[k];
+    r.pos_lo[k] = (float)(c.pos[k] - (double)r.pos_hi[k]);
   }
   r.dt = f.dt;
   r.dt32 = (float)f.dt;
+  r.dt_hi = r.dt32;
+  r.dt_lo = (float)(f.dt - (double)r.dt_hi);
   r.K = f.K;
   r.nx = c.nx;
   r.ny = c.ny;

@@ -83,13 +83,14 @@ void destroy_cube_device(birp_cube& c) {
   if (c.alloc_stream) {
     // stream-ordered pool memory: no device-wide synchronisation on release
     for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
-                    (void*)c.d_grid, (void*)c.d_walk4})
+                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff})
       if (p) cudaFreeAsync(p, c.alloc_stream);
   } else {
     for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
-                    (void*)c.d_grid, (void*)c.d_walk4})
+                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff})
       if (p) cudaFree(p);
   }
+  c.d_nodes_ff = nullptr;
   c.d_grid = nullptr;
   c.d_walk4 = nullptr;
   c.d_cells = nullptr;
@@ -181,9 +182,11 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
   }
   CKU(dev_alloc(&c.d_c64, coords * sizeof(double), c.alloc_stream));
+  CKU(dev_alloc(&c.d_nodes_ff, (coords + 6) * sizeof(float2), c.alloc_stream));
   if (!lut.empty()) CKU(dev_alloc(&c.d_lut, lut.size() * sizeof(float4), c.alloc_stream));
   CKU(dev_alloc(&c.d_desc, sizeof(CubeDev), c.alloc_stream));
-  c.device_bytes = coords * sizeof(double) + lut.size() * sizeof(float4) + sizeof(CubeDev) +
+  c.device_bytes = coords * sizeof(double) + (coords + 6) * sizeof(float2) + lut.size() * sizeof(float4) +
+                   sizeof(CubeDev) +
                    (compact ? total * sizeof(float) + walk.size() * sizeof(float4)
                             : records * 2 * sizeof(float4) + walk2.size() * sizeof(float2));
 
@@ -202,6 +205,22 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   all.reserve(coords);
   for (int k = 0; k < 3; ++k) all.insert(all.end(), c.c[k].begin(), c.c[k].end());
   CKU(cudaMemcpyAsync(c.d_c64, all.data(), coords * sizeof(double), cudaMemcpyHostToDevice, st));
+  // node coordinates as float pairs, each axis between sentinels -inf / +inf
+  // (a walk past the last plane finds no crossing)
+  std::vector<float2> nodes_ff;
+  nodes_ff.reserve(coords + 6);
+  size_t ff_off[3];
+  for (int k = 0, o = 0; k < 3; o += c.n[k], ++k) {
+    nodes_ff.push_back(make_float2(-INFINITY, 0.f));
+    ff_off[k] = nodes_ff.size();
+    for (int i = 0; i < c.n[k]; ++i) {
+      const double v = all[o + i];
+      const float h = (float)v;
+      nodes_ff.push_back(make_float2(h, (float)(v - (double)h)));
+    }
+    nodes_ff.push_back(make_float2(INFINITY, 0.f));
+  }
+  CKU(cudaMemcpyAsync(c.d_nodes_ff, nodes_ff.data(), nodes_ff.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
   if (compact) {
     CKU(cudaMemcpyAsync(c.d_walk4, walk.data(), walk.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
   } else {
@@ -229,6 +248,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     a.c_first = ck[0];
     a.c_last = ck[a.n - 1];
     a.c64 = c.d_c64 + off;
+    d.nodes_ff[k] = c.d_nodes_ff + ff_off[k];
     off += a.n;
   }
   d.rec = c.d_vals;
@@ -270,8 +290,10 @@ size_t cube_device_bytes(const birp_cube& c) {
       lut += (size_t)std::max(1.0, std::ceil((c.c[k].back() - c.c[k].front()) / c.min_gap[k])) * sizeof(float4);
   const size_t walk = 2 * (coords + 3) + 1;
   const size_t records = ((size_t)c.n[0] + 1) * ((size_t)c.n[1] + 1) * ((size_t)c.n[2] + 1);
-  const size_t layout_bytes = c.layout == BIRP_CUBE_COMPACT ? total * sizeof(float) + walk * sizeof(float4)
-                                                            : records * 2 * sizeof(float4) + walk * sizeof(float2);
+  const size_t nodes_ff = (coords + 6) * sizeof(float2);
+  const size_t layout_bytes = nodes_ff + (c.layout == BIRP_CUBE_COMPACT
+                                              ? total * sizeof(float) + walk * sizeof(float4)
+                                              : records * 2 * sizeof(float4) + walk * sizeof(float2));
   return layout_bytes + coords * sizeof(double) + lut + sizeof(CubeDev);
 }
 }  // namespace birp

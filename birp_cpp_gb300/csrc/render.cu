@@ -34,6 +34,12 @@ namespace birp {
 namespace {
 
 constexpr int kThreads = 128;
+#ifndef BIRP_WALK_MINB
+#define BIRP_WALK_MINB 8  // resident CTAs per SM of the cube-walk batch kernels
+#endif
+#ifndef BIRP_NEAREST_MINB
+#define BIRP_NEAREST_MINB 8  // resident CTAs per SM of the nearest-mode batch kernel
+#endif
 #ifndef BIRP_CMEM_MINB
 #define BIRP_CMEM_MINB 6  // resident CTAs per SM the CMEM batch kernel is compiled for
 #endif
@@ -88,6 +94,40 @@ __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
   s = a + b;
   float bp = s - a;
   e = (a - (s - bp)) + (b - bp);
+}
+
+// Float-float arithmetic: a value is hi + lo with |lo| <= ulp(hi) / 2 (about
+// 48 significant bits), built from FP32 FMAs. The nearest-mode walk locates
+// its cell crossings in it, at 1/58 of the cost of FP64 on this GPU; results
+// within the stated bound of a decision boundary are redone in FP64.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_quick(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+  float s, e;
+  two_sum(x.hi, y.hi, s, e);
+  return ff_quick(s, e + (x.lo + y.lo));
+}
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+  const float p = x.hi * y.hi;
+  const float e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
+  return ff_quick(p, e);
+}
+// 1/x: one Newton step r + r (1 - x r) from the FP32 reciprocal
+__device__ __forceinline__ FF ff_recip(FF x) {
+  const float r = 1.f / x.hi;
+  const FF t = ff_mul(x, {r, 0.f});
+  return ff_quick(r, r * ((1.f - t.hi) - t.lo));
+}
+// 1/sqrt(x): one Newton step r + r/2 (1 - x r^2) from the FP32 estimate
+__device__ __forceinline__ FF ff_rsqrt(FF x) {
+  const float r = rsqrtf(x.hi);
+  const FF t = ff_mul(x, ff_mul({r, 0.f}, {r, 0.f}));
+  return ff_quick(r, 0.5f * r * ((1.f - t.hi) - t.lo));
 }
 
 // FP64 sample position of the FP64 oracle: pos + d * ((i + 0.5) * dt).
@@ -351,13 +391,39 @@ __device__ int exact_cell(const AxisDev& a, double x, int guess) {
   return k;
 }
 
+// First sample index i in [lo, hi] past the plane c along one axis, by the
+// FP64 oracle's own position pos64(i) = p + d ((i + 1/2) dt): moving up, past
+// means pos64 >= c; moving down, pos64 < c (hi if none in [lo, hi)). The
+// predicate is monotone in i. Not inlined: it runs only when a float-float
+// crossing lies within its error bound of an integer.
+__device__ __noinline__ int exact_first_past(double p, double d, double dt, double c, bool up, int lo, int hi) {
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    const double x = pos64(p, d, dt, mid);
+    if (up ? (x >= c) : (x < c)) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+// The same, with the ray's FP64 direction rebuilt from the tile's column and
+// row terms (a, b: the oracle's w = a + b, normalised as dir64 does), so the
+// caller's walk keeps no FP64 state live.
+__device__ __noinline__ int exact_first_past_ray(const double* a, const double* b, int axis, double p, double dt,
+                                                 double c, bool up, int lo, int hi) {
+  double w[3], d[3];
+  for (int r = 0; r < 3; ++r) w[r] = __dadd_rn(a[r], b[r]);
+  dir64(w, d);
+  return exact_first_past(p, d[axis], dt, c, up, lo, hi);
+}
+
 // ---------------------------------------------------------------- one tile
 
 enum Interp { NEAREST = 0, TRILINEAR = 1 };
-// Axis handling of the cube march: UNIFORM computes the index affinely, LUT
-// through the index tables, DDA walks cell by cell along the ray (any axes;
-// trilinear only).
-// AXES_DDA_COMPACT is the same walk over a compact-layout cube.
+// Axis handling of the cube march: cubes are walked cell by cell along the
+// ray (AXES_DDA over the records layout, AXES_DDA_COMPACT over the compact
+// layout; trilinear and nearest). UNIFORM (affine index) is the template
+// value CMEM requests carry.
 enum Axes { AXES_UNIFORM = 0, AXES_LUT = 1, AXES_DDA = 2, AXES_DDA_COMPACT = 3 };
 
 // One pixel tile of one request. The lanes-per-ray split S = 2^seg_log2 is a
@@ -419,7 +485,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   const int N = R.N;
   int a = 0, b = N;
   // per-lane telemetry, summed over the warp at the end (one atomic per warp)
-  unsigned int n_exact = 0, n_cells = 0;
+  unsigned int n_exact = 0, n_cells = 0, n_exact_nearest = 0;
   if constexpr (KIND == SPACE_CUBE) {
     const CubeDev& C = *R.cube;
     AxisEst est[3];
@@ -479,7 +545,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
   const float fS = (float)S;
 
   int nsamp = iters;  // samples this lane evaluates (for the counters)
-  if constexpr (KIND == SPACE_CUBE && (AXES == AXES_DDA || AXES == AXES_DDA_COMPACT)) {
+  if constexpr (KIND == SPACE_CUBE && INTERP == TRILINEAR) {
+    static_assert(AXES == AXES_DDA || AXES == AXES_DDA_COMPACT, "cubes march with AXES_DDA[_COMPACT]");
     constexpr bool COMPACT = AXES == AXES_DDA_COMPACT;
     // Cell-space integration. A lane takes a contiguous run of its ray's
     // samples and walks the cells the run crosses. Per axis the sample
@@ -621,81 +688,155 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       n_cells = (unsigned int)ncell;
     }
   } else if constexpr (KIND == SPACE_CUBE) {
-    // nearest by truncation (UNIFORM / LUT index)
+    // Nearest by truncation, walked cell by cell. A sample takes the value of
+    // the lower node of the cell that holds it (DataCube::GetSample,
+    // src/DataCube.cpp:203-277, with the exact per-cell lookup of the FP64
+    // oracle), so a cell contributes value * (its sample count). The field
+    // jumps at every node plane, so each sample must land in the cell the
+    // FP64 oracle picks: the first sample past a plane P along an axis is
+    // i* = ceil(u) with u = (P - p) / (d dt) - 1/2 (first i with p + d (i+1/2)
+    // dt >= P moving up, < P moving down), computed in float-float with error
+    // bound E; when u is within E of an integer the oracle's FP64 predicate
+    // decides (a bracketed search over pos64). The lane's first cell is
+    // located the same way. All counts are exact integers.
+    constexpr bool COMPACT = AXES == AXES_DDA_COMPACT;
     const CubeDev& C = *R.cube;
-    // node k's value: the first corner of cell k's record (records layout,
-    // 8 floats per record) or the padded grid's node (compact layout)
-    const bool cmp = C.compact != 0;
-    const float* __restrict__ vals = cmp ? C.grid : reinterpret_cast<const float*>(C.rec);
-    const int cxn = cmp ? (int)C.gx : (int)C.cx, cxyn = cmp ? (int)C.gxy : (int)C.cxy;
-    const int vmul = cmp ? 1 : 8;
-    const int hi0 = C.ax[0].n - 1, hi1 = C.ax[1].n - 1, hi2 = C.ax[2].n - 1;
-    float st[3], bs[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      if constexpr (AXES == AXES_UNIFORM) {
-        st[k] = R.dt32 * d32[k] * C.ax[k].inv_h;
-        bs[k] = fmaf(0.5f, st[k], R.oidx[k]);
-      } else {
-        st[k] = R.dt32 * d32[k];
-        bs[k] = fmaf(0.5f, st[k], R.pos32[k]);
-      }
-    }
-    // nearest: FP32 index error bound in cells, linear in the sample index:
-    // direction error over t, coordinate rounding, index rounding (|idx| <= n)
-    float eps_slope = 0.f, eps_base = 0.f;
-    if constexpr (INTERP == NEAREST) {
-      float inv_hmin = 0.f, n_max = 0.f;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        float ih = (AXES == AXES_UNIFORM) ? C.ax[k].inv_h : C.ax[k].lut_inv_w;
-        inv_hmin = fmaxf(inv_hmin, ih);
-        n_max = fmaxf(n_max, (float)C.ax[k].n);
-      }
-      float apos = fabsf(R.pos32[0]) + fabsf(R.pos32[1]) + fabsf(R.pos32[2]);
-      eps_slope = R.dt32 * (kDirErr + 5e-7f) * inv_hmin;
-      eps_base = (0.5f * R.dt32 * (kDirErr + 5e-7f) + apos * 5e-7f) * inv_hmin + n_max * 5e-7f + 1e-5f;
-    }
-#pragma unroll 2
-    for (int it = 0; it < iters; ++it) {
-      float idx[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        if constexpr (AXES == AXES_UNIFORM) {
-          idx[k] = fmaf(fi, st[k], bs[k]);
-        } else {
-          idx[k] = lut_index(C.ax[k], C.lut, fmaf(fi, st[k], bs[k]));
-        }
-      }
-      int bx, by, bz;
-      float flx = magic_floor(idx[0], bx);
-      float fly = magic_floor(idx[1], by);
-      float flz = magic_floor(idx[2], bz);
-      float fx = idx[0] - flx, fy = idx[1] - fly, fz = idx[2] - flz;
-      float v;
-      static_assert(INTERP == NEAREST, "trilinear cubes march with AXES_DDA");
+    const int total = b - a;
+    const int seglen = (total + S - 1) >> SEGL2;
+    const int first_c = a + min(seg * seglen, total);
+    const int count = max(0, min(total - seg * seglen, seglen));
+    nsamp = count;
+    unsigned int n_fp64 = 0;
+    if (count > 0) {
+      // Per axis: 1 / (d dt) and K = p / (d dt) + 1/2 as float pairs, so the
+      // crossing index of plane P is u = P / (d dt) - K; the error bound E of
+      // u; a pointer to the next plane's node in the float-pair table (the
+      // +-inf sentinels end the walk; an axis the ray does not move along
+      // points at +inf and has no crossing)
+      FF inv[3], K[3];
+      float E32[3], cp[3];  // FP32 error bound of u; |coordinates| + |p| for the float-float bound
+      const float2* np[3];
+      int kc[3];
       {
-        float eps_cell = fmaf(fi, eps_slope, eps_base);
-        bool unsure = !(fminf(fminf(fx, 1.f - fx), fminf(fminf(fy, 1.f - fy), fminf(fz, 1.f - fz))) >= eps_cell);
-        if (unsure) {
-          // decide the cell exactly as the FP64 oracle does
-          need_d64();
-          int i = first + (it << SEGL2);
-          int cx = exact_cell(C.ax[0], pos64(R.pos[0], d64[0], R.dt, i), bx - kMagicBits);
-          int cy = exact_cell(C.ax[1], pos64(R.pos[1], d64[1], R.dt, i), by - kMagicBits);
-          int cz = exact_cell(C.ax[2], pos64(R.pos[2], d64[2], R.dt, i), bz - kMagicBits);
-          bx = cx + kMagicBits;
-          by = cy + kMagicBits;
-          bz = cz + kMagicBits;
-          if (stats) atomicAdd(&stats->exact_nearest, 1ull);
+        FF w[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const float h = (float)w64[k];
+          w[k] = {h, (float)(w64[k] - (double)h)};
         }
-        const int ix = min(max(bx - kMagicBits, -1), hi0), iy = min(max(by - kMagicBits, -1), hi1),
-                  iz = min(max(bz - kMagicBits, -1), hi2);
-        v = __ldg(vals + vmul * record_index(cxn, cxyn, ix, iy, iz));
+        const FF rs = ff_rsqrt(ff_add(ff_add(ff_mul(w[0], w[0]), ff_mul(w[1], w[1])), ff_mul(w[2], w[2])));
+        const FF dtf = {R.dt_hi, R.dt_lo};
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const AxisDev& A = C.ax[k];
+          if (w[k].hi != 0.f) {
+            inv[k] = ff_recip(ff_mul(ff_mul(w[k], rs), dtf));
+            K[k] = ff_add(ff_mul({R.pos_hi[k], R.pos_lo[k]}, inv[k]), {0.5f, 0.f});
+          } else {
+            inv[k] = {1.f, 0.f};
+            K[k] = {0.f, 0.f};
+          }
+          cp[k] = fmaxf(fabsf((float)A.c_first), fabsf((float)A.c_last)) + fabsf(R.pos32[k]);
+          // FP32 estimate fma(P_hi, inv_hi, -K_hi): P_hi, inv_hi, K_hi each
+          // within 2^-24 relative of their exact values (K ~ p inv) and one
+          // final rounding of |u| <= N + 2: < 2.4e-7 (|P| + |p|) |inv| + 6e-8 |u|
+          E32[k] = fmaf(3e-7f * cp[k], fabsf(inv[k].hi), fmaf(1.2e-7f, (float)(N + 2), 1e-5f));
+        }
       }
-      acc.add(v);
-      fi += fS;
+      // first global sample index in [0, N) past the plane of node pointer
+      // `nd` along axis k, or kNever when no sample of the ray is past it (a
+      // sentinel plane, or a crossing at or after N): a walk never steps past
+      // a sentinel
+      constexpr int kNever = 0x3fffffff;
+      auto cross = [&](int k, const float2* nd) -> int {
+        const float2 P = __ldg(nd);
+        // FP32 estimate first; float-float only within its bound of an integer
+        const float u32 = fmaf(P.x, inv[k].hi, -K[k].hi);
+        if (!(u32 <= (float)N + 1.5f)) return kNever;  // also NaN: a sentinel plane
+        if (u32 < -1.5f) return 0;
+        const float m0 = rintf(u32);
+        const float d32u = u32 - m0;
+        if (fabsf(d32u) > E32[k]) {
+          const int i = max((int)m0 + (d32u > 0.f ? 1 : 0), 0);
+          return i < N ? i : kNever;
+        }
+        const FF u = ff_add(ff_mul({P.x, P.y}, inv[k]), {-K[k].hi, -K[k].lo});
+        const float n0 = rintf(u.hi);
+        const float dist = (u.hi - n0) + u.lo;
+        // representation of P and p (2^-47 relative each, also covering the
+        // cancellation in P / (d dt) - K), the relative error of u (direction,
+        // reciprocal: < 3e-13) and the oracle's own FP64 rounding of the
+        // position, in sample-index units
+        const float E = fmaf(1e-14f * cp[k], fabsf(inv[k].hi), fmaf(3e-13f, (float)(N + 2), 1e-9f));
+        int i;
+        if (fabsf(dist) > E) {
+          i = max((int)n0 + (dist > 0.f ? 1 : 0), 0);
+        } else {
+          // within the bound: the oracle's predicate decides
+          ++n_fp64;
+          const double c = C.ax[k].c64[nd - C.nodes_ff[k]];
+          const float uc = u.hi + u.lo;
+          i = exact_first_past_ray(sm.A[lx], sm.B[ly], k, R.pos[k], R.dt, c, inv[k].hi > 0.f,
+                                   max((int)floorf(uc - E) - 1, 0), min((int)ceilf(uc + E) + 2, N));
+        }
+        return i < N ? i : kNever;
+      };
+      // the lane's first cell, exactly; then the next plane on each axis
+      int nxtc[3], dstr[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const AxisDev& A = C.ax[k];
+        const float2* nodes = C.nodes_ff[k];
+        const float x0 = fmaf((float)first_c + 0.5f, R.dt32 * d32[k], R.pos32[k]);
+        const float idx = A.uniform ? (x0 - A.c0) * A.inv_h : lut_index(A, C.lut, x0);
+        int kb;
+        magic_floor(fminf(fmaxf(idx, 0.f), (float)(A.n - 2)), kb);
+        int kk = kb - kMagicBits;
+        const bool up = inv[k].hi > 0.f;
+        if (w64[k] == 0.0) {
+          // d = 0 on this axis: every sample sits at pos64 = p + 0
+          kk = exact_cell(A, pos64(R.pos[k], 0.0, R.dt, first_c), kk);
+          np[k] = nodes + A.n;  // +inf: no crossing
+        } else {
+          if (up) {
+            for (int g = 0; g < A.n && kk > 0 && cross(k, nodes + kk) > first_c; ++g) --kk;
+            for (int g = 0; g < A.n && kk < A.n - 2 && cross(k, nodes + kk + 1) <= first_c; ++g) ++kk;
+          } else {
+            for (int g = 0; g < A.n && kk > 0 && cross(k, nodes + kk) <= first_c; ++g) --kk;
+            for (int g = 0; g < A.n && kk < A.n - 2 && cross(k, nodes + kk + 1) > first_c; ++g) ++kk;
+          }
+          np[k] = nodes + (up ? kk + 1 : kk);  // the next plane: node kk + 1 up, kk down
+        }
+        kc[k] = kk;
+        nxtc[k] = cross(k, np[k]) - first_c;
+        const int stride = COMPACT ? (int)record_stride(C.gx, C.gxy, k) : 8 * (int)record_stride(C.cx, C.cxy, k);
+        dstr[k] = up ? stride : -stride;  // in floats
+      }
+      // node value pointer: the padded grid (compact) or the first float of
+      // the cell's record (8 floats); cells stay within [-1, n-1], whose data
+      // exist, because a walk stops at the sentinel planes
+      const float* q = COMPACT ? C.grid + record_index(C.gx, C.gxy, kc[0], kc[1], kc[2])
+                               : reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, kc[0], kc[1], kc[2]);
+      int u = 0;
+      const int cap = count + C.ax[0].n + C.ax[1].n + C.ax[2].n + 4;
+      for (int guard = 0; u < count && guard < cap; ++guard) {
+        const int nxt = min(min(min(nxtc[0], nxtc[1]), nxtc[2]), count);
+        if (nxt > u) {
+          acc.add(__ldg(q) * (float)(nxt - u));
+          u = nxt;
+        }
+        if (u >= count) break;  // the run is summed: no further steps
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          while (nxtc[k] <= u) {  // ends at a sentinel plane (kNever)
+            q += dstr[k];
+            np[k] += (dstr[k] > 0) ? 1 : -1;
+            nxtc[k] = cross(k, np[k]) - first_c;
+          }
+        }
+      }
     }
+    n_exact_nearest = n_fp64;
   } else {
     const CmemDev& M = *R.cmem;
     float st[3], bs[3];
@@ -732,6 +873,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     const unsigned int cc = __reduce_add_sync(0xffffffffu, n_cells);
     if (lane == 0 && ce) atomicAdd(&stats->exact_range_rays, (unsigned long long)ce);
     if (lane == 0 && cc) atomicAdd(&stats->cells, (unsigned long long)cc);
+    const unsigned int cn = __reduce_add_sync(0xffffffffu, n_exact_nearest);
+    if (lane == 0 && cn) atomicAdd(&stats->exact_nearest, (unsigned long long)cn);
   }
   // merge the S partial sums of a ray
   float hi = acc.s, lo = -acc.c;
@@ -761,10 +904,10 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
   } else if (R.interp) {
     if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
     else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, st);
-  } else if (R.axes_lut) {
-    render_tile<SPACE_CUBE, NEAREST, AXES_LUT>(R, tx, ty, sm, st);
+  } else if (R.compact) {
+    render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
   } else {
-    render_tile<SPACE_CUBE, NEAREST, AXES_UNIFORM>(R, tx, ty, sm, st);
+    render_tile<SPACE_CUBE, NEAREST, AXES_DDA>(R, tx, ty, sm, st);
   }
 }
 
@@ -774,7 +917,10 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
 // first). CLS = BATCH_CUBE_TRI compiles only the trilinear cube march (fewer
 // registers, more resident warps); BATCH_ANY renders every request kind.
 template <int CLS>
-__global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY ? 1 : CLS == BATCH_CMEM ? BIRP_CMEM_MINB : 8)
+__global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
+                                           : CLS == BATCH_CMEM         ? BIRP_CMEM_MINB
+                                           : CLS == BATCH_CUBE_NEAREST ? BIRP_NEAREST_MINB
+                                                                       : BIRP_WALK_MINB)
     render_batch_kernel(BatchDev B) {
   __shared__ TileSmem sm;
   __shared__ int s_item;
@@ -802,6 +948,9 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY ? 1 : CLS == BATCH_
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CMEM) {
       render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM>(R, tx, ty, sm, B.stats);
+    } else if constexpr (CLS == BATCH_CUBE_NEAREST) {
+      if (R.compact) render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
+      else render_tile<SPACE_CUBE, NEAREST, AXES_DDA>(R, tx, ty, sm, B.stats);
     } else {
       render_tile_any(R, tx, ty, sm, B.stats);
     }
@@ -1031,8 +1180,8 @@ cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStr
   else if (h.interp && h.compact)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, stats);
   else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, stats);
-  else if (h.axes_lut) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_LUT><<<grid, kThreads, 0, s>>>(h, stats);
-  else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_UNIFORM><<<grid, kThreads, 0, s>>>(h, stats);
+  else if (h.compact) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, stats);
+  else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA><<<grid, kThreads, 0, s>>>(h, stats);
   return cudaGetLastError();
 }
 
@@ -1046,6 +1195,8 @@ int persistent_grid(int cls) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI_COMPACT>, kThreads, 0);
   else if (cls == BATCH_CMEM)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CMEM>, kThreads, 0);
+  else if (cls == BATCH_CUBE_NEAREST)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_NEAREST>, kThreads, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_ANY>, kThreads, 0);
   if (per_sm < 1) per_sm = 1;
@@ -1056,6 +1207,7 @@ cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int
   if (cls == BATCH_CUBE_TRI) render_batch_kernel<BATCH_CUBE_TRI><<<grid, kThreads, 0, s>>>(b);
   else if (cls == BATCH_CUBE_TRI_COMPACT) render_batch_kernel<BATCH_CUBE_TRI_COMPACT><<<grid, kThreads, 0, s>>>(b);
   else if (cls == BATCH_CMEM) render_batch_kernel<BATCH_CMEM><<<grid, kThreads, 0, s>>>(b);
+  else if (cls == BATCH_CUBE_NEAREST) render_batch_kernel<BATCH_CUBE_NEAREST><<<grid, kThreads, 0, s>>>(b);
   else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b);
   return cudaGetLastError();
 }
