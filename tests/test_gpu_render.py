@@ -81,6 +81,29 @@ def test_axis_parallel_rays_exact(birp, oracle):
             assert np.array_equal(img, ref), (pos, march, int((img != ref).sum()))
 
 
+@pytest.mark.parametrize("layout", [0, 1])
+def test_nearest_axis_parallel_random_field(birp, oracle, layout):
+    """Nearest mode with rays nearly parallel to grid planes (camera on an
+    axis, narrow field) on a random field: a sample counted in the wrong cell
+    would move a pixel by ~1/N relative, far above the tolerance, so this
+    checks the float-float / FP64 crossing decisions where they are hardest."""
+    rng = np.random.default_rng(12)
+    xs = np.linspace(-8, 8, 33)
+    ys = np.concatenate([np.linspace(-8, -2, 7), np.linspace(-1.5, 8, 20)])
+    vals = rng.uniform(0.5, 1.5, (len(xs), len(ys), len(xs)))
+    g = birp.Cube(xs, ys, xs, vals.astype(np.float32), layout=layout)
+    oc = oracle.Cube64(xs, ys, xs, vals.astype(np.float32).astype(np.float64), 0)
+    for pos, aim in [((-7.5, 0.0, 0.0), (5.0, 0, 0)), ((0.0, -6.0, 0.0), (0.0, 0, 0)), ((0.0, 0.0, 7.9), (0.0, 0, 0)),
+                     ((-7.75, 0.25, -0.5), (5.0, 0, 0))]:
+        for march in (birp.PREFIX, birp.CLIP):
+            cam = birp.camera(pos, aim, 2.0, 2.0, 33, 33, n_samples=1760, march=march, trilinear=False)
+            img = birp.render(g, cam)
+            ref = oracle.render64(oc, o_cam(oracle, cam), threads=THREADS)
+            mx, rms, n = rel_err(img, ref)
+            assert mx <= TOL, (pos, march, layout, mx)
+    g.close()
+
+
 @pytest.mark.parametrize("march", [0, 1])
 @pytest.mark.parametrize("tri", [True, False])
 def test_config0_cube(birp, oracle, cube0, march, tri):
