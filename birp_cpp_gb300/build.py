@@ -63,9 +63,28 @@ def build(verbose: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     build_classes()
+    build_cli()
     if verbose:
-        print("built", LIB, "and", CLASSES_LIB)
+        print("built", LIB, CLASSES_LIB, "and", CLI)
     return LIB
+
+
+CLI = os.path.join(LIBDIR, "birp")
+
+
+def build_cli() -> str:
+    """The command-line front-end (cli/birp.cpp) over the classes: lib/birp."""
+    src = os.path.join(HERE, "cli", "birp.cpp")
+    deps = [src, CLASSES_LIB] + [os.path.join(CPP, "include", "birp", h)
+                                 for h in os.listdir(os.path.join(CPP, "include", "birp"))]
+    if os.path.exists(CLI) and all(os.path.getmtime(CLI) >= os.path.getmtime(d) for d in deps):
+        return CLI
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", src, "-I", os.path.join(CPP, "include"), "-L", LIBDIR,
+           "-lbirp_classes", "-lbirp_gb300", "-lpthread", "-Wl,-rpath,$ORIGIN", "-o", CLI]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return CLI
 
 
 def build_classes() -> str:

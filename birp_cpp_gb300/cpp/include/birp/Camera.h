@@ -34,6 +34,8 @@ class Camera {
   int Height() const { return image_dimension_y; }
 
  private:
+  friend void RenderBatch(const std::vector<Camera*>& cameras);
+  birp_camera Describe() const;  // this camera as the C ABI's request
   int image_dimension_x;
   int image_dimension_y;
   float fov_x;
@@ -47,3 +49,9 @@ class Camera {
   int march = 0;
   int segments = 0;
 };
+
+// Renders several cameras (any mix of DataCubes and CMEM) in one batched GPU
+// launch (birp_batch_render); each camera's image accumulates its render, as
+// Render() does. No reference counterpart: the reference renders one camera
+// per call (src/main.cpp:242-264).
+void RenderBatch(const std::vector<Camera*>& cameras);

@@ -4,8 +4,7 @@
 // fused GB300 kernels instead of calling GetSample per sample.
 #pragma once
 
-struct birp_cube;
-struct birp_cmem;
+#include "../../../../include/birp_gb300.h"  // the C ABI the classes call
 
 class Space {
  public:

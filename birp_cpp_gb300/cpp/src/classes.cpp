@@ -159,8 +159,18 @@ void DataCube::Upload() {
       std::memcpy(flat.data() + (k * ny + j) * nx, slices[k][j].data(), nx * sizeof(float));
     }
   }
-  check(birp_cube_create(xs[0].data(), (int)nx, xs[1].data(), (int)ny, xs[2].data(), (int)nz, flat.data(), &gpu));
+  check(birp_cube_create_layout(xs[0].data(), (int)nx, xs[1].data(), (int)ny, xs[2].data(), (int)nz, flat.data(),
+                                layout, &gpu));
   InitMeta();
+}
+
+void DataCube::SetLayout(int l) {
+  if (l != BIRP_CUBE_RECORDS && l != BIRP_CUBE_COMPACT) throw std::invalid_argument("unknown cube layout");
+  if (l != layout && gpu) {  // rebuilt on next use
+    birp_cube_destroy(gpu);
+    gpu = nullptr;
+  }
+  layout = l;
 }
 
 const birp_cube* DataCube::GpuCube() {
@@ -276,8 +286,7 @@ void Camera::SetMarchMode(int mode) { march = mode; }
 
 void Camera::SetSegments(int lanes) { segments = lanes; }
 
-void Camera::Render() {
-  ensure_init();
+birp_camera Camera::Describe() const {
   birp_camera c;
   std::memset(&c, 0, sizeof c);
   c.pos[0] = position.x;
@@ -295,14 +304,58 @@ void Camera::Render() {
   c.trilinear = dataCube->Trilinear() ? 1 : 0;
   c.march = march;
   c.segments = segments;
-  const birp_cube* cube = dataCube->GpuCube();
-  const birp_cmem* cmem = cube ? nullptr : dataCube->GpuCmem();
+  return c;
+}
+
+namespace {
+
+// the GPU source of a Space: exactly one of cube / cmem
+void gpu_source(Space* s, const birp_cube*& cube, const birp_cmem*& cmem) {
+  cube = s->GpuCube();
+  cmem = cube ? nullptr : s->GpuCmem();
   if (!cube && !cmem) throw std::invalid_argument("this Space has no GPU representation (DataCube or CMEM)");
+}
+
+// the reference accumulates into image (src/Camera.cpp:223)
+void accumulate(std::vector<std::vector<float>>& image, const float* out, int nx, int ny) {
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nx; ++i) image[j][i] = image[j][i] + out[(size_t)j * nx + i];
+}
+
+}  // namespace
+
+void Camera::Render() {
+  ensure_init();
+  const birp_camera c = Describe();
+  const birp_cube* cube;
+  const birp_cmem* cmem;
+  gpu_source(dataCube, cube, cmem);
   std::vector<float> out((size_t)c.nx * c.ny);
   check(birp_render(cube, cmem, &c, out.data(), nullptr));
-  // the reference accumulates into image (src/Camera.cpp:223)
-  for (int j = 0; j < c.ny; ++j)
-    for (int i = 0; i < c.nx; ++i) image[j][i] = image[j][i] + out[(size_t)j * c.nx + i];
+  accumulate(image, out.data(), c.nx, c.ny);
+}
+
+void RenderBatch(const std::vector<Camera*>& cameras) {
+  ensure_init();
+  if (cameras.empty()) return;
+  std::vector<birp_request> reqs(cameras.size());
+  std::vector<std::vector<float>> outs(cameras.size());
+  std::vector<float*> ptrs(cameras.size());
+  int64_t pixels = 0;
+  for (size_t i = 0; i < cameras.size(); ++i) {
+    reqs[i].cam = cameras[i]->Describe();
+    gpu_source(cameras[i]->dataCube, reqs[i].cube, reqs[i].cmem);
+    outs[i].resize((size_t)reqs[i].cam.nx * reqs[i].cam.ny);
+    ptrs[i] = outs[i].data();
+    pixels += (int64_t)outs[i].size();
+  }
+  birp_batch* b = nullptr;
+  check(birp_batch_create((int)cameras.size(), pixels, &b));
+  const birp_status st = birp_batch_render(b, reqs.data(), (int)reqs.size(), ptrs.data());
+  birp_batch_destroy(b);
+  check(st);
+  for (size_t i = 0; i < cameras.size(); ++i)
+    accumulate(cameras[i]->image, outs[i].data(), reqs[i].cam.nx, reqs[i].cam.ny);
 }
 
 int Camera::ToDat(std::string filename) {
