@@ -89,11 +89,12 @@ def build_cli() -> str:
 
 def build_classes() -> str:
     """The reference-API C++ classes (cpp/) over the C ABI: libbirp_classes.so."""
-    src = os.path.join(CPP, "src", "classes.cpp")
-    deps = [src, LIB] + [os.path.join(CPP, "include", "birp", h) for h in os.listdir(os.path.join(CPP, "include", "birp"))]
+    srcs = [os.path.join(CPP, "src", f) for f in ("classes.cpp", "helper.cpp")]
+    deps = srcs + [LIB] + [os.path.join(CPP, "include", "birp", h)
+                           for h in os.listdir(os.path.join(CPP, "include", "birp"))]
     if os.path.exists(CLASSES_LIB) and all(os.path.getmtime(CLASSES_LIB) >= os.path.getmtime(d) for d in deps):
         return CLASSES_LIB
-    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", src, "-I", os.path.join(CPP, "include"),
+    cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", *srcs, "-I", os.path.join(CPP, "include"),
            "-L", LIBDIR, "-lbirp_gb300", "-Wl,-rpath,$ORIGIN", "-o", CLASSES_LIB]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -1,8 +1,8 @@
 #!/bin/sh
 # Builds oracle/_ref/libbirp_ref.so from the UNMODIFIED reference sources
 # where they lie (src/Camera.cpp, DataCube.cpp, Cmem.cpp, Helper.cpp), plus
-# the no-op EleFits headers in oracle/ref_shim and the C wrapper
-# oracle/ref_capi.cpp. Test infrastructure only (pins the oracle and makes the
+# the no-op EleFits headers in oracle/ref_shim and the C wrappers
+# oracle/ref_capi.cpp and oracle/helper_shim.cpp. Test infrastructure only (pins the oracle and makes the
 # golden fixtures); the reference tree exists only in the development
 # container, so this is skipped elsewhere.
 set -e
@@ -19,5 +19,5 @@ mkdir -p "$OUT"
 g++ -O3 -std=c++23 -fPIC -shared -w \
   -I"$HERE/ref_shim" -I"$REF/include" \
   "$REF/src/Camera.cpp" "$REF/src/DataCube.cpp" "$REF/src/Cmem.cpp" "$REF/src/Helper.cpp" \
-  "$HERE/ref_capi.cpp" -o "$OUT/libbirp_ref.so"
+  "$HERE/ref_capi.cpp" "$HERE/helper_shim.cpp" -o "$OUT/libbirp_ref.so"
 echo "built $OUT/libbirp_ref.so"
