@@ -250,12 +250,14 @@ def run_c4(args, B):
                 pass
             k += 1
             nxt += rng.exponential(1.0 / rate)
-        lat = [r.latency_ms for r in (srv.wait(t, 120000) for t in tickets) if r.status == 0]
+        done = [r for r in (srv.wait(t, 120000) for t in tickets) if r.status == 0]
         t1 = time.perf_counter()
         st1 = srv.stats()
-        lat = np.array(lat) if lat else np.zeros(1)
-        results.append({"offered_req_s": rate, "completed": len(lat), "images_s": len(lat) / (t1 - t0),
+        lat = np.array([r.latency_ms for r in done]) if done else np.zeros(1)
+        qms = np.array([r.queue_ms for r in done]) if done else np.zeros(1)
+        results.append({"offered_req_s": rate, "completed": len(done), "images_s": len(done) / (t1 - t0),
                         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                        "queue_p99_ms": float(np.percentile(qms, 99)),
                         "uploads": st1.cube_uploads - st0.cube_uploads, "evictions": st1.cube_evictions - st0.cube_evictions,
                         "hits": st1.cube_hits - st0.cube_hits, "rejected": st1.rejected - st0.rejected})
         print(json.dumps(results[-1]), flush=True)

@@ -273,7 +273,9 @@ void prefault_outputs(float* const* dst, const size_t* floats, int n) {
   size_t total = 0;
   for (int i = 0; i < n; ++i) total += dst[i] ? floats[i] : 0;
   const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
-  const int nt = (int)std::min<size_t>({8, hw, total / (1u << 22) + 1});  // >= 16 MB per thread
+  // >= 128 MB per thread: when the pages are mapped already (the usual case
+  // for reused buffers) the touch is ~1 store per page, cheaper than a thread
+  const int nt = (int)std::min<size_t>({8, hw, total / (1u << 25) + 1});
   auto work = [&](int t) {
     for (int i = t; i < n; i += nt) {
       if (!dst[i] || !floats[i]) continue;

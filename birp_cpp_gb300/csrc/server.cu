@@ -2,13 +2,16 @@
 //
 // Requests are admitted as they arrive. A scheduler thread forms a batch from
 // the pending queue whenever a slot (a batch object with its own stream and
-// CUDA graph) is free, making each batch's cubes resident first: cubes live in
-// GPU memory under a byte budget, least-recently-used cubes that no in-flight
-// batch references are evicted, and a missing cube is re-uploaded from its
-// pinned host copy on a separate stream (stream-ordered pool allocations, so
-// neither upload nor eviction synchronises the device). Batches on different
-// slots overlap on the GPU. One completion thread per slot waits for its
-// batch, copies each image to the caller's buffer and completes the tickets.
+// CUDA graph) is free, taking requests whose source is resident. Cubes live in
+// GPU memory under a byte budget; a request for a cube that is not resident
+// waits while an uploader thread brings the cube in (evicting
+// least-recently-used cubes that no in-flight batch references, re-uploading
+// from the pinned host copy on a separate stream, with stream-ordered pool
+// allocations so neither upload nor eviction synchronises the device) — the
+// other requests keep being batched meanwhile. Batches on different slots
+// overlap on the GPU. One completion thread per slot waits for its batch,
+// copies each image to the caller's buffer unless the kernels wrote it there,
+// and completes the tickets.
 // The reference has no counterpart: its only "many renders" path is the
 // serial directory loop of src/main.cpp:242-264.
 #include <algorithm>
@@ -40,6 +43,8 @@ struct Source {
   birp_cube* resident = nullptr;
   uint64_t last_use = 0;
   int in_use = 0;           // batches (forming or in flight) that reference it
+  bool uploading = false;   // queued for or in the uploader
+  birp_status upload_err = BIRP_OK;  // the last upload's failure, reported once
   birp_cmem* cmem = nullptr;
 };
 
@@ -68,8 +73,10 @@ struct Slot {
 struct birp_server {
   birp_server_config cfg{};
   std::mutex mu;
-  std::condition_variable cv_sched, cv_done;
+  std::condition_variable cv_sched, cv_done, cv_upload;
   std::deque<Req*> pending;
+  std::deque<int> upload_q;  // sources to make resident, in request order
+  std::thread uploader;
   std::unordered_map<int64_t, Req*> tickets;
   std::vector<Source> sources;
   std::vector<Slot*> slots;
@@ -90,20 +97,14 @@ void finish(birp_server* s, Req* r, birp_status status) {
   r->done = true;
 }
 
-// Makes source `id` resident; called with the lock held, releases it around
-// the upload itself. Returns BIRP_OK or an error for the requests of `id`.
-birp_status make_resident(birp_server* s, int id, std::unique_lock<std::mutex>& lk) {
+// Frees budget for source `id` by evicting least-recently-used resident
+// cubes that no batch references; called with the lock held. BIRP_ERR_BUSY
+// when the budget is held by in-flight batches (retry later).
+birp_status make_room(birp_server* s, int id) {
   Source& src = s->sources[id];
-  src.last_use = ++s->tick;
-  if (src.kind != 0) return BIRP_OK;
-  if (src.resident) {
-    s->st.cube_hits++;
-    return BIRP_OK;
-  }
   if (src.bytes > s->cfg.cube_budget_bytes)
     return fail(BIRP_ERR_NOMEM, "cube needs %lld B, budget is %lld B", (long long)src.bytes,
                 (long long)s->cfg.cube_budget_bytes);
-  // evict least-recently-used cubes that no batch references
   while (s->resident_bytes + src.bytes > s->cfg.cube_budget_bytes) {
     int victim = -1;
     for (int i = 0; i < (int)s->sources.size(); ++i) {
@@ -111,7 +112,7 @@ birp_status make_resident(birp_server* s, int id, std::unique_lock<std::mutex>& 
       if (i == id || !o.resident || o.in_use > 0) continue;
       if (victim < 0 || o.last_use < s->sources[victim].last_use) victim = i;
     }
-    if (victim < 0) return fail(BIRP_ERR_BUSY, "cube budget held by in-flight batches");
+    if (victim < 0) return BIRP_ERR_BUSY;
     Source& v = s->sources[victim];
     birp_cube* c = v.resident;
     v.resident = nullptr;
@@ -120,28 +121,56 @@ birp_status make_resident(birp_server* s, int id, std::unique_lock<std::mutex>& 
     destroy_cube_device(*c);  // stream-ordered release on the upload stream
     delete c;
   }
-  // upload outside the lock (the source is pinned by in_use)
-  birp_cube* c = new birp_cube();
-  c->layout = s->cfg.cube_layout;
-  birp_status rc = BIRP_OK;
-  s->resident_bytes += src.bytes;
-  const float* vals = src.h_vals;
-  std::vector<double> ax[3] = {src.ax[0], src.ax[1], src.ax[2]};
-  lk.unlock();
-  for (int k = 0; k < 3 && rc == BIRP_OK; ++k) rc = analyze_axis(ax[k].data(), (int)ax[k].size(), "xyz"[k], *c, k);
-  if (rc == BIRP_OK) rc = upload_cube(*c, vals, s->upload_stream, true);
-  lk.lock();
-  if (rc != BIRP_OK) {
-    s->resident_bytes -= src.bytes;
-    destroy_cube_device(*c);
-    delete c;
-    return rc;
-  }
-  s->resident_bytes += (int64_t)c->device_bytes - src.bytes;
-  src.bytes = (int64_t)c->device_bytes;
-  src.resident = c;
-  s->st.cube_uploads++;
   return BIRP_OK;
+}
+
+// Uploader thread: makes the queued cubes resident one at a time, with the
+// lock released during the upload itself, and wakes the scheduler.
+void uploader_loop(birp_server* s) {
+  std::unique_lock<std::mutex> lk(s->mu);
+  while (!s->stop) {
+    if (s->upload_q.empty()) {
+      s->cv_upload.wait(lk);
+      continue;
+    }
+    const int id = s->upload_q.front();
+    birp_status rc = make_room(s, id);
+    if (rc == BIRP_ERR_BUSY) {  // wait for a batch to finish, then retry
+      s->cv_upload.wait_for(lk, std::chrono::milliseconds(1));
+      continue;
+    }
+    s->upload_q.pop_front();
+    Source& src = s->sources[id];
+    if (rc == BIRP_OK) {
+      birp_cube* c = new birp_cube();
+      c->layout = s->cfg.cube_layout;
+      const int64_t reserved = src.bytes;
+      s->resident_bytes += reserved;
+      const float* vals = src.h_vals;
+      std::vector<double> ax[3] = {src.ax[0], src.ax[1], src.ax[2]};
+      lk.unlock();
+      for (int k = 0; k < 3 && rc == BIRP_OK; ++k)
+        rc = analyze_axis(ax[k].data(), (int)ax[k].size(), "xyz"[k], *c, k);
+      if (rc == BIRP_OK) rc = upload_cube(*c, vals, s->upload_stream, true);
+      lk.lock();
+      Source& done = s->sources[id];  // (the vector may have grown meanwhile)
+      s->resident_bytes -= reserved;
+      if (rc == BIRP_OK) {
+        s->resident_bytes += (int64_t)c->device_bytes;
+        done.bytes = (int64_t)c->device_bytes;
+        done.resident = c;
+        done.last_use = ++s->tick;
+        s->st.cube_uploads++;
+      } else {
+        destroy_cube_device(*c);
+        delete c;
+      }
+    }
+    Source& done = s->sources[id];
+    done.upload_err = rc;
+    done.uploading = false;
+    s->cv_sched.notify_all();
+  }
 }
 
 void slot_worker(birp_server* s, Slot* slot) {
@@ -151,8 +180,9 @@ void slot_worker(birp_server* s, Slot* slot) {
     if (!slot->has_work) return;
     lk.unlock();
     birp_status rc = batch_wait(slot->batch);
-    // copy images to the callers' buffers (outside the lock)
-    if (rc == BIRP_OK)
+    // copy images to the callers' buffers (outside the lock) unless the
+    // kernels wrote them there
+    if (rc == BIRP_OK && !slot->batch->direct)
       for (size_t i = 0; i < slot->reqs.size(); ++i)
         std::memcpy(slot->reqs[i]->out, slot->batch->h_out + slot->batch->offsets[i],
                     (size_t)slot->batch->npx[i] * sizeof(float));
@@ -166,6 +196,7 @@ void slot_worker(birp_server* s, Slot* slot) {
     slot->busy = false;
     s->cv_done.notify_all();
     s->cv_sched.notify_all();
+    s->cv_upload.notify_all();  // budget an uploader waits for may be free now
   }
 }
 
@@ -191,72 +222,63 @@ void scheduler_loop(birp_server* s) {
         continue;
       }
     }
-    // form a batch in arrival order
-    std::vector<Req*> take;
-    std::vector<int> srcs;
+    // form a batch in arrival order from requests whose source is resident;
+    // a request for a cube that is not resident stays pending while the
+    // uploader brings the cube in
+    std::vector<Req*> go;
+    std::vector<int> used_srcs;
     int64_t px = 0;
-    std::deque<Req*> keep;
-    while (!s->pending.empty() && (int)take.size() < s->cfg.max_batch_requests) {
+    std::deque<Req*> waiting;
+    std::vector<int> failed;  // sources whose upload failure this scan reports
+    while (!s->pending.empty() && (int)go.size() < s->cfg.max_batch_requests) {
       Req* r = s->pending.front();
       int64_t n = (int64_t)r->cam.nx * r->cam.ny;
       if (n > s->cfg.max_batch_pixels) {  // can never fit
         s->pending.pop_front();
         fail(BIRP_ERR_INVALID, "image larger than the batch pixel limit");
         finish(s, r, BIRP_ERR_INVALID);
+        s->st.completed++;
         s->cv_done.notify_all();
+        continue;
+      }
+      Source& src = s->sources[r->src];
+      if (src.kind == 0 && !src.resident) {
+        s->pending.pop_front();
+        if (src.upload_err != BIRP_OK) {  // the upload for it failed
+          finish(s, r, src.upload_err);
+          s->st.completed++;
+          s->cv_done.notify_all();
+          if (std::find(failed.begin(), failed.end(), r->src) == failed.end()) failed.push_back(r->src);
+          continue;
+        }
+        if (!src.uploading) {
+          src.uploading = true;
+          s->upload_q.push_back(r->src);
+          s->cv_upload.notify_one();
+        }
+        waiting.push_back(r);
         continue;
       }
       if (px + n > s->cfg.max_batch_pixels) break;
       s->pending.pop_front();
-      take.push_back(r);
+      go.push_back(r);
       px += n;
-      if (std::find(srcs.begin(), srcs.end(), r->src) == srcs.end()) {
-        srcs.push_back(r->src);
-        s->sources[r->src].in_use++;
+      if (std::find(used_srcs.begin(), used_srcs.end(), r->src) == used_srcs.end()) {
+        used_srcs.push_back(r->src);
+        src.in_use++;  // no eviction while this batch references it
+        src.last_use = ++s->tick;
+        if (src.kind == 0) s->st.cube_hits++;
       }
     }
-    if (take.empty()) continue;
-    slot->busy = true;  // reserve the slot while cubes upload
-    // residency
-    std::vector<char> src_ok(s->sources.size(), 1);
-    std::vector<birp_status> src_err(s->sources.size(), BIRP_OK);
-    for (int id : srcs) {
-      birp_status rc = make_resident(s, id, lk);
-      if (rc == BIRP_ERR_BUSY) {
-        // budget held by other batches: retry these requests later
-        src_ok[id] = 0;
-      } else if (rc != BIRP_OK) {
-        src_ok[id] = 0;
-        src_err[id] = rc;
-      }
-    }
-    std::vector<Req*> go;
-    std::vector<birp_request> reqs;
-    for (Req* r : take) {
-      if (src_ok[r->src]) {
-        go.push_back(r);
-        continue;
-      }
-      if (src_err[r->src] != BIRP_OK) {
-        finish(s, r, src_err[r->src]);
-        s->st.completed++;
-      } else {
-        keep.push_back(r);
-      }
-    }
-    for (auto it = keep.rbegin(); it != keep.rend(); ++it) s->pending.push_front(*it);
-    std::vector<int> used_srcs;
-    for (int id : srcs) {
-      bool used = std::any_of(go.begin(), go.end(), [&](Req* r) { return r->src == id; });
-      if (used) used_srcs.push_back(id);
-      else s->sources[id].in_use--;
-    }
-    s->cv_done.notify_all();
-    if (go.empty()) {
-      slot->busy = false;
-      if (!keep.empty()) s->cv_sched.wait_for(lk, std::chrono::milliseconds(1));
+    for (auto it = waiting.rbegin(); it != waiting.rend(); ++it) s->pending.push_front(*it);
+    // a failure is reported to the requests pending now; later ones retry
+    for (int id : failed) s->sources[id].upload_err = BIRP_OK;
+    if (go.empty()) {  // every pending request waits for an upload
+      s->cv_sched.wait(lk);
       continue;
     }
+    slot->busy = true;
+    std::vector<birp_request> reqs;
     for (Req* r : go) {
       birp_request q{};
       const Source& src = s->sources[r->src];
@@ -265,8 +287,14 @@ void scheduler_loop(birp_server* s) {
       q.cam = r->cam;
       reqs.push_back(q);
     }
+    // where the device writes pageable host memory, the kernels write each
+    // request's image straight into its caller's buffer (no copy-out)
+    std::vector<float*> direct;
+    if (host_direct_writes())
+      for (Req* r : go) direct.push_back(r->out);
     const auto now = Clock::now();
-    birp_status rc = batch_submit(slot->batch, reqs.data(), (int)reqs.size());
+    birp_status rc =
+        batch_submit(slot->batch, reqs.data(), (int)reqs.size(), direct.empty() ? nullptr : direct.data());
     for (Req* r : go) r->t_launch = now;
     s->st.batches++;
     slot->reqs = go;
@@ -337,6 +365,7 @@ birp_status birp_server_create(const birp_server_config* cfg, birp_server** out)
     s->slots.push_back(sl);
   }
   for (Slot* sl : s->slots) sl->worker = std::thread(slot_worker, s, sl);
+  s->uploader = std::thread(uploader_loop, s);
   s->scheduler = std::thread(scheduler_loop, s);
   *out = s;
   return ok();
@@ -348,9 +377,11 @@ birp_status birp_server_destroy(birp_server* s) {
     std::lock_guard<std::mutex> lk(s->mu);
     s->stop = true;
     s->cv_sched.notify_all();
+    s->cv_upload.notify_all();
     for (Slot* sl : s->slots) sl->cv.notify_all();
   }
   if (s->scheduler.joinable()) s->scheduler.join();
+  if (s->uploader.joinable()) s->uploader.join();
   for (Slot* sl : s->slots) {
     // a batch still in flight is waited for by its worker before it exits
     {
