@@ -107,12 +107,10 @@ struct RequestDev {
   int seg_log2;      // rays are split over 2^seg_log2 lanes
   int tiles_x;       // tiles along x for this request's tile shape
   int tiles;         // total tiles
-  int axes_lut;      // cube: 1 when any axis needs the LUT
   int compact;       // cube: 1 in the compact layout (node values, no records)
   const CubeDev* cube;   // device pointer (kind == SPACE_CUBE)
   const CmemDev* cmem;   // device pointer (kind == SPACE_CMEM)
   float* out;            // ny*nx floats, row 0 = top
-  float oidx[3];         // (pos - c0) * inv_h for uniform axes
 };
 
 // Status/counters the kernels report (device memory, read by the host).

@@ -229,10 +229,7 @@ birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const bi
   r.out = out;
   if (cube) {
     r.cube = cube->d_desc;
-    r.axes_lut = cube->h_desc.all_uniform ? 0 : 1;
     r.compact = cube->h_desc.compact;
-    for (int k = 0; k < 3; ++k)
-      r.oidx[k] = cube->uniform[k] ? (float)((c.pos[k] - cube->c[k][0]) * cube->inv_h[k]) : 0.f;
   } else {
     r.cmem = cmem->d_desc;
   }

@@ -420,11 +420,10 @@ __device__ __noinline__ int exact_first_past_ray(const double* a, const double* 
 // ---------------------------------------------------------------- one tile
 
 enum Interp { NEAREST = 0, TRILINEAR = 1 };
-// Axis handling of the cube march: cubes are walked cell by cell along the
-// ray (AXES_DDA over the records layout, AXES_DDA_COMPACT over the compact
-// layout; trilinear and nearest). UNIFORM (affine index) is the template
-// value CMEM requests carry.
-enum Axes { AXES_UNIFORM = 0, AXES_LUT = 1, AXES_DDA = 2, AXES_DDA_COMPACT = 3 };
+// Cube layout of the march: cubes are walked cell by cell along the ray
+// (AXES_DDA over the records layout, AXES_DDA_COMPACT over the compact layout;
+// trilinear and nearest). CMEM requests carry AXES_NONE.
+enum Axes { AXES_NONE = 0, AXES_DDA = 2, AXES_DDA_COMPACT = 3 };
 
 // One pixel tile of one request. The lanes-per-ray split S = 2^seg_log2 is a
 // runtime value of the request (it only sets the tile shape, the lane -> ray
@@ -900,7 +899,7 @@ __global__ void __launch_bounds__(kThreads) render_plain_kernel(const RequestDev
 // Dispatch over the request's variant.
 __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& sm, KernelStats* st) {
   if (R.kind == SPACE_CMEM) {
-    render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM>(R, tx, ty, sm, st);
+    render_tile<SPACE_CMEM, TRILINEAR, AXES_NONE>(R, tx, ty, sm, st);
   } else if (R.interp) {
     if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
     else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, st);
@@ -947,7 +946,7 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
     } else if constexpr (CLS == BATCH_CUBE_TRI_COMPACT) {
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CMEM) {
-      render_tile<SPACE_CMEM, TRILINEAR, AXES_UNIFORM>(R, tx, ty, sm, B.stats);
+      render_tile<SPACE_CMEM, TRILINEAR, AXES_NONE>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CUBE_NEAREST) {
       if (R.compact) render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
       else render_tile<SPACE_CUBE, NEAREST, AXES_DDA>(R, tx, ty, sm, B.stats);
@@ -1176,7 +1175,7 @@ int tile_h(int segl2) { return th_of(segl2); }
 
 cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStream_t s) {
   dim3 grid((h.nx + tw_of(h.seg_log2) - 1) / tw_of(h.seg_log2), (h.ny + th_of(h.seg_log2) - 1) / th_of(h.seg_log2));
-  if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_UNIFORM><<<grid, kThreads, 0, s>>>(h, stats);
+  if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_NONE><<<grid, kThreads, 0, s>>>(h, stats);
   else if (h.interp && h.compact)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, stats);
   else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, stats);
