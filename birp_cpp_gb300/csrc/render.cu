@@ -254,14 +254,18 @@ struct CmemDir {
   float r, theta, ct, st, cp, sp, b2;  // b2 = 2 / (1 + cos theta)
 };
 
+// sqrt(x) for x >= 0 from the hardware reciprocal square root (a few ulp;
+// exact 0 at 0, where x * rsqrt(x) would be 0 * inf)
+__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+
 __device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
   CmemDir d;
   const float ryz2 = fmaf(y, y, z * z);
-  const float ryz = sqrtf(ryz2);
-  d.r = sqrtf(fmaf(x, x, ryz2));
+  const float ryz = sqrt_fast(ryz2);
+  d.r = sqrt_fast(fmaf(x, x, ryz2));
   if (x != 0.f) {
     d.theta = atan2f(ryz, x);
-    const float ir = 1.f / d.r;
+    const float ir = __fdividef(1.f, d.r);
     d.ct = x * ir;
     d.st = ryz * ir;
     d.b2 = x >= 0.f ? 2.f * d.r / (d.r + x) : 2.f * d.r * (d.r - x) / ryz2;
@@ -272,7 +276,7 @@ __device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
     d.b2 = 1.f;
   }
   if (y != 0.f) {
-    const float iyz = 1.f / ryz;
+    const float iyz = __fdividef(1.f, ryz);
     d.cp = y * iyz;
     d.sp = fabsf(z) * iyz;
   } else {
@@ -291,11 +295,11 @@ __device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d,
   const float ux = d.ct, uy = d.st * d.cp, uz = d.st * d.sp;
   float dn = ux * m.cos_tn + uz * m.sin_tn;
   float cnx = uy * m.sin_tn, cny = uz * m.cos_tn - ux * m.sin_tn, cnz = -uy * m.cos_tn;
-  float phi_n = atan2f(sqrtf(cnx * cnx + cny * cny + cnz * cnz), dn);
+  float phi_n = atan2f(sqrt_fast(cnx * cnx + cny * cny + cnz * cnz), dn);
   float ds = ux * m.cos_ts - uz * m.sin_ts;
   float csx = -uy * m.sin_ts, csy = uz * m.cos_ts + ux * m.sin_ts, csz = -uy * m.cos_ts;
-  float phi_s = atan2f(sqrtf(csx * csx + csy * csy + csz * csz), ds);
-  const float ch = sqrtf(1.f / d.b2);  // cos(theta / 2)
+  float phi_s = atan2f(sqrt_fast(csx * csx + csy * csy + csz * csz), ds);
+  const float ch = rsqrtf(d.b2);  // cos(theta / 2); b2 >= 1
   float base = ch + m.a5 * (2.f * d.st * d.ct) * (1.f - exp2f(-kLog2e * d.theta));
   float f = pow_pos(base, m.p1 * (m.bc0 + m.bc1 * d.cp + m.bc3 * (d.sp * d.sp)));
   float q = m.p2c * exp2f(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
@@ -305,7 +309,7 @@ __device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d,
   float ry = m.bs * exp2f(m.ay * lb);
   float rz = m.bs * exp2f(m.az * lb);
   float a1 = rz * d.cp, a2 = ry * d.sp;
-  r_bs = (ry * rz) / sqrtf(a1 * a1 + a2 * a2);
+  r_bs = (ry * rz) * rsqrtf(a1 * a1 + a2 * a2);  // cp^2 + sp^2 = 1: the sum is > 0
 }
 
 __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
@@ -321,7 +325,7 @@ __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, floa
   float h4 = (h * h) * (h * h);
   float sheath = m.A1 * exp2f(-kLog2e * m.B * h4) * pow_pos(r * 0.1f, -m.alpha - m.beta * (d.st * d.st));
   float d10 = r * 0.1f;
-  float outer = m.A2 / (d10 * d10 * d10);
+  float outer = __fdividef(m.A2, d10 * d10 * d10);
   float v;
   if (r < r_mp - half) v = 0.f;
   else if (r >= r_mp - half && r <= r_mp + half) v = lerp_f(0.f, sheath, (r - (r_mp - half)) / (r_mp + half));
