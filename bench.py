@@ -544,10 +544,10 @@ def main():
             "ray_samples_per_s": samples_per_step * world / (step_ms / 1000.0),
             "roofline": roofline, "roofline_per_sample": roofline_per_sample, "roofline_hbm": roofline_hbm,
             "cpu_baseline": cpu, "parity": parity,
-            # each step replays one graph with three kernels: the general one
-            # and the compact-layout one (no work here) and the records-layout
+            # each step replays one graph with four kernels: the CMEM, nearest
+            # and compact-layout ones (no work here) and the records-layout
             # trilinear one
-            "gpu_launches": 3 * args.steps, "clocks": clocks.summary(),
+            "gpu_launches": 4 * args.steps, "clocks": clocks.summary(),
             "exact_fp64_rays_per_step": ks["exact_range_rays"] / args.steps,
             "samples_per_cell": (ks["samples"] / ks["cells"]) if ks.get("cells") else None,
         }
