@@ -26,6 +26,8 @@ struct birp_cube {
   float* d_grid = nullptr;      // compact layout: padded node values
   float4* d_walk4 = nullptr;    // compact layout: walk tables with inverse widths
   float2* d_nodes_ff = nullptr; // node coordinates as float pairs, 3 axes concatenated
+  int has_neg = -1;             // a value below zero (-1: not yet known)
+  uint8_t* d_negflag = nullptr; // its negative-value flags (CubeDev::negflag)
   size_t device_bytes = 0;
   cudaStream_t alloc_stream = nullptr;  // non-null: stream-ordered (pool) allocations
 };
@@ -87,6 +89,8 @@ birp_status analyze_axis(const double* c, int n, char name, birp_cube& cube, int
 birp_status upload_cube(birp_cube& cube, const float* values, cudaStream_t stream, bool stream_alloc);
 // estimate of the device bytes a cube of these dims will hold
 size_t cube_device_bytes(const birp_cube& cube);
+// whether any of the n values is below zero (a NaN is not)
+bool any_negative(const float* v, size_t n);
 void destroy_cube_device(birp_cube& cube);
 birp_status ensure_xyz_scratch(size_t floats);
 

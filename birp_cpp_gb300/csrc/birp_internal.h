@@ -72,6 +72,15 @@ struct CubeDev {
   uint32_t gxy;         // (nx + 2) * (ny + 2)
   const float4* walk4_up[3];
   const float4* walk4_dn[3];
+  // cubes holding a value below zero (nullptr otherwise): one byte per node
+  // (i, j, k), x fastest, 1 when a node in [i-1, i+2] x [j-1, j+2] x
+  // [k-1, k+2] is negative, i.e. when the cell with lower node (i, j, k) or a
+  // neighbour of it has a negative corner; with the largest |coordinate|, the
+  // inverse of the smallest cell width and the most nodes over the three axes
+  // (the bound on how far an FP32 cell index can be off)
+  const uint8_t* negflag;
+  float neg_cmax, neg_inv_gap;
+  int neg_nmax;
 };
 
 // CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
@@ -156,6 +165,7 @@ enum BatchClass : int {
 cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
+cudaError_t launch_cube_negflags(const float* padded, int nx, int ny, int nz, uint8_t* flags, cudaStream_t stream);
 cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, const double* cx64, const double* cy64,
                                 const double* cz64, float4* rec, cudaStream_t stream);
 cudaError_t launch_cube_sample(const CubeDev* cube, int trilinear, const float* xyz, int n, float* out,

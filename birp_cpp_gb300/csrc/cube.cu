@@ -66,6 +66,25 @@ static void build_lut(const std::vector<double>& c, double w, std::vector<float4
   }
 }
 
+bool any_negative(const float* v, size_t n) {
+  // sign bits first, per chunk (a loop the compiler vectorises); a chunk with
+  // one set (-0.0, a negative value or a NaN) is tested exactly
+  constexpr size_t kChunk = 1 << 16;
+  for (size_t i0 = 0; i0 < n; i0 += kChunk) {
+    const size_t i1 = std::min(n, i0 + kChunk);
+    uint32_t sign = 0;
+    for (size_t i = i0; i < i1; ++i) {
+      uint32_t b;
+      std::memcpy(&b, v + i, sizeof b);
+      sign |= b;
+    }
+    if (sign & 0x80000000u)
+      for (size_t i = i0; i < i1; ++i)
+        if (v[i] < 0.f) return true;
+  }
+  return false;
+}
+
 birp_status ensure_xyz_scratch(size_t floats) {
   Context& g = g_ctx;
   if (g.xyz_floats >= floats) return BIRP_OK;
@@ -83,13 +102,14 @@ void destroy_cube_device(birp_cube& c) {
   if (c.alloc_stream) {
     // stream-ordered pool memory: no device-wide synchronisation on release
     for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
-                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff})
+                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff, (void*)c.d_negflag})
       if (p) cudaFreeAsync(p, c.alloc_stream);
   } else {
     for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
-                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff})
+                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff, (void*)c.d_negflag})
       if (p) cudaFree(p);
   }
+  c.d_negflag = nullptr;
   c.d_nodes_ff = nullptr;
   c.d_grid = nullptr;
   c.d_walk4 = nullptr;
@@ -117,6 +137,8 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   const int nx = c.n[0], ny = c.n[1], nz = c.n[2];
   const size_t px = (size_t)nx + 2, py = (size_t)ny + 2, pz = (size_t)nz + 2;
   const size_t total = px * py * pz;
+  const size_t nodes = (size_t)nx * ny * nz;
+  if (c.has_neg < 0) c.has_neg = any_negative(values, nodes) ? 1 : 0;
   if (!st) st = g_ctx.stream;
   c.alloc_stream = stream_alloc ? st : nullptr;
 
@@ -185,8 +207,9 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   CKU(dev_alloc(&c.d_nodes_ff, (coords + 6) * sizeof(float2), c.alloc_stream));
   if (!lut.empty()) CKU(dev_alloc(&c.d_lut, lut.size() * sizeof(float4), c.alloc_stream));
   CKU(dev_alloc(&c.d_desc, sizeof(CubeDev), c.alloc_stream));
+  if (c.has_neg) CKU(dev_alloc(&c.d_negflag, nodes, c.alloc_stream));
   c.device_bytes = coords * sizeof(double) + (coords + 6) * sizeof(float2) + lut.size() * sizeof(float4) +
-                   sizeof(CubeDev) +
+                   sizeof(CubeDev) + (c.has_neg ? nodes : 0) +
                    (compact ? total * sizeof(float) + walk.size() * sizeof(float4)
                             : records * 2 * sizeof(float4) + walk2.size() * sizeof(float2));
 
@@ -200,6 +223,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   p.kind = cudaMemcpyHostToDevice;
   CKU(cudaMemcpy3DAsync(&p, st));
   CKU(launch_cube_fill(nullptr, nx, ny, nz, scalar, st));
+  if (c.has_neg) CKU(launch_cube_negflags(scalar, nx, ny, nz, c.d_negflag, st));
   // (the host vectors below stay alive until the synchronize at the end)
   std::vector<double> all;
   all.reserve(coords);
@@ -251,6 +275,17 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     d.nodes_ff[k] = c.d_nodes_ff + ff_off[k];
     off += a.n;
   }
+  d.negflag = c.d_negflag;
+  if (c.has_neg) {
+    double cmax = 0.0, inv_gap = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      cmax = std::max({cmax, std::abs(c.c[k].front()), std::abs(c.c[k].back())});
+      inv_gap = std::max(inv_gap, 1.0 / c.min_gap[k]);
+      d.neg_nmax = std::max(d.neg_nmax, c.n[k]);
+    }
+    d.neg_cmax = (float)cmax;
+    d.neg_inv_gap = (float)inv_gap;
+  }
   d.rec = c.d_vals;
   d.cx = (uint32_t)(nx + 1);
   d.cxy = (uint32_t)((nx + 1) * (ny + 1));
@@ -294,6 +329,7 @@ size_t cube_device_bytes(const birp_cube& c) {
   const size_t layout_bytes = nodes_ff + (c.layout == BIRP_CUBE_COMPACT
                                               ? total * sizeof(float) + walk * sizeof(float4)
                                               : records * 2 * sizeof(float4) + walk * sizeof(float2));
-  return layout_bytes + coords * sizeof(double) + lut + sizeof(CubeDev);
+  const size_t negflag = c.has_neg > 0 ? (size_t)c.n[0] * c.n[1] * c.n[2] : 0;
+  return layout_bytes + coords * sizeof(double) + lut + sizeof(CubeDev) + negflag;
 }
 }  // namespace birp

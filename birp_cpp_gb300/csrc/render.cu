@@ -421,6 +421,97 @@ __device__ __noinline__ int exact_first_past_ray(const double* a, const double* 
   return exact_first_past(p, d[axis], dt, c, up, lo, hi);
 }
 
+// ---------------------------------------------------------------- negative values
+
+// std::lerp in FP64 as libstdc++ defines it (the FP64 oracle interpolates with
+// std::lerp): t b + (1 - t) a when a and b do not share a sign, else
+// a + t (b - a) kept monotone next to b; every operation rounded separately.
+__device__ __forceinline__ double lerp64(double a, double b, double t) {
+  if ((a <= 0.0 && b >= 0.0) || (a >= 0.0 && b <= 0.0)) return __dadd_rn(__dmul_rn(t, b), __dmul_rn(__dsub_rn(1.0, t), a));
+  if (t == 1.0) return b;
+  const double x = __dadd_rn(a, __dmul_rn(t, __dsub_rn(b, a)));
+  return ((t > 1.0) == (b > a)) ? (b < x ? x : b) : (b > x ? x : b);
+}
+
+// Node (i, j, k)'s input value in either layout: the padded grid, or c0 of
+// the record of the cell whose lower corner it is (exactly the FP32 input).
+__device__ __forceinline__ double node_value(const CubeDev& C, int i, int j, int k) {
+  return C.compact ? (double)__ldg(C.grid + record_index(C.gx, C.gxy, i, j, k))
+                   : (double)__ldg(reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, i, j, k));
+}
+
+// Whether in-box sample i of a ray is below zero in the FP64 oracle's own
+// arithmetic (cube64_sample at pos64, direction rebuilt from the tile's
+// column/row terms a + b): the exact cell of each coordinate (g: the FP32
+// guesses), FP64 fractions and lerps x -> y -> z, or the lower node's value
+// for nearest. Not inlined: it runs only for samples in flagged cells.
+__device__ __noinline__ bool sample_negative64(const CubeDev* Cp, int trilinear, const double* a, const double* b,
+                                               double px, double py, double pz, double dt, int i, int g0, int g1,
+                                               int g2) {
+  const CubeDev& C = *Cp;
+  double w[3], d[3];
+  for (int r = 0; r < 3; ++r) w[r] = __dadd_rn(a[r], b[r]);
+  dir64(w, d);
+  const double P[3] = {px, py, pz};
+  const int g[3] = {g0, g1, g2};
+  double p[3], f[3];
+  int k[3];
+  for (int r = 0; r < 3; ++r) {
+    p[r] = pos64(P[r], d[r], dt, i);
+    k[r] = exact_cell(C.ax[r], p[r], g[r]);
+  }
+  if (!trilinear) return node_value(C, k[0], k[1], k[2]) < 0.0;
+  for (int r = 0; r < 3; ++r) {
+    const double* c = C.ax[r].c64;
+    f[r] = __ddiv_rn(__dsub_rn(p[r], c[k[r]]), __dsub_rn(c[k[r] + 1], c[k[r]]));
+  }
+  auto v = [&](int di, int dj, int dk) { return node_value(C, k[0] + di, k[1] + dj, k[2] + dk); };
+  const double lx1 = lerp64(v(0, 0, 0), v(1, 0, 0), f[0]), lx2 = lerp64(v(0, 1, 0), v(1, 1, 0), f[0]);
+  const double hx1 = lerp64(v(0, 0, 1), v(1, 0, 1), f[0]), hx2 = lerp64(v(0, 1, 1), v(1, 1, 1), f[0]);
+  return lerp64(lerp64(lx1, lx2, f[1]), lerp64(hx1, hx2, f[1]), f[2]) < 0.0;
+}
+
+// First sample in [lo, hi) of this lane's ray that is below zero (want_neg)
+// or not (!want_neg); hi if none. The ray's S lanes test S consecutive
+// samples per step and stop together at the first hit. A sample is tested in
+// FP64 only when its FP32 cell is flagged (the flags cover one cell around
+// every negative corner, and the FP32 cell is within one of the exact cell
+// unless all_exact, which tests every sample). Every lane of the warp calls.
+// (d0..d2: the ray's FP32 direction; a / b: the tile terms of its FP64
+// direction.) Inlined: a call costs the walks more in saved registers.
+__device__ __forceinline__ int neg_search(const RequestDev* Rp, float d0, float d1, float d2, const double* a,
+                                       const double* b, int S, int seg, int lo, int hi, bool want_neg,
+                                       bool all_exact) {
+  const RequestDev& R = *Rp;
+  const CubeDev& C = *R.cube;
+  const float st[3] = {R.dt32 * d0, R.dt32 * d1, R.dt32 * d2};
+  int found = hi;
+  for (int base = lo; __any_sync(0xffffffffu, base < found); base += S) {
+    const int i = base + seg;
+    bool hit = false;
+    if (base < found && i < hi) {
+      int g[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const AxisDev& A = C.ax[k];
+        const float x = fmaf((float)i + 0.5f, st[k], R.pos32[k]);
+        const float idx = A.uniform ? (x - A.c0) * A.inv_h : lut_index(A, C.lut, x);
+        int kb;
+        magic_floor(fminf(fmaxf(idx, 0.f), (float)(A.n - 2)), kb);
+        g[k] = kb - kMagicBits;
+      }
+      bool neg = false;
+      if (all_exact || __ldg(C.negflag + ((size_t)g[2] * C.ax[1].n + g[1]) * C.ax[0].n + g[0]))
+        neg = sample_negative64(R.cube, R.interp, a, b, R.pos[0], R.pos[1], R.pos[2], R.dt, i, g[0], g[1], g[2]);
+      hit = neg == want_neg;
+    }
+    int cand = hit ? i : hi;
+    for (int o = S >> 1; o >= 1; o >>= 1) cand = min(cand, __shfl_xor_sync(0xffffffffu, cand, o));
+    found = min(found, cand);
+  }
+  return found;
+}
+
 // ---------------------------------------------------------------- one tile
 
 enum Interp { NEAREST = 0, TRILINEAR = 1 };
@@ -540,6 +631,35 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     if (b < a) b = a;
   }
   if (!valid) { a = 0; b = 0; }
+  if constexpr (KIND == SPACE_CUBE) {
+    // A value below zero ends the run as the box edge does: the reference
+    // stops at its first sample < 0 (src/Camera.cpp:205-209), the -1 outside
+    // the box and negative field values alike. Cubes holding a negative value
+    // carry flags; their rays look for the first negative sample of the
+    // in-box run (PREFIX), or skip negative samples to the first good one and
+    // then look for the next negative (CLIP), before the run is summed.
+    const CubeDev& C = *R.cube;
+    if (C.negflag) {
+      // bound on |FP32 cell index - exact index|: position error (step,
+      // position and coordinate roundings) over the smallest cell, the
+      // index rounding and the uniform-axis tolerance; one cell or more and
+      // the flags' one-cell margin does not cover it
+      const float e_pos = 4e-7f * ((float)N * R.dt32 + fabsf(R.pos32[0]) + fabsf(R.pos32[1]) + fabsf(R.pos32[2]) +
+                                   C.neg_cmax) + 1e-6f;
+      const bool all_exact = fmaf(e_pos, C.neg_inv_gap, 2e-6f * (float)C.neg_nmax + 1e-6f) >= 1.f;
+      const double* ta = sm.A[lx];
+      const double* tb = sm.B[ly];
+      auto search = [&](int lo, int hi, bool want_neg) {
+        return neg_search(&R, d32[0], d32[1], d32[2], ta, tb, S, seg, lo, hi, want_neg, all_exact);
+      };
+      if (R.mode == MARCH_PREFIX) {
+        b = search(a, b, true);
+      } else {
+        a = search(a, b, false);
+        b = search(a, b, true);
+      }
+    }
+  }
 
   Kahan acc;
   const int first = a + seg;
@@ -895,7 +1015,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 
 // One request, one CTA per tile; the request travels as a kernel parameter.
 template <int KIND, int INTERP, int AXES>
-__global__ void __launch_bounds__(kThreads) render_plain_kernel(const RequestDev req, KernelStats* stats) {
+__global__ void __launch_bounds__(kThreads) render_plain_kernel(const __grid_constant__ RequestDev req,
+                                                                KernelStats* stats) {
   __shared__ TileSmem sm;
   render_tile<KIND, INTERP, AXES>(req, blockIdx.x, blockIdx.y, sm, stats);
 }
@@ -1022,6 +1143,23 @@ __global__ void cube_records_kernel(const float* __restrict__ v, int nx, int ny,
     const double c7 = (((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000))) * (ix * iy * iz);
     rec[2 * r] = make_float4((float)v000, (float)c1, (float)c2, (float)c4);
     rec[2 * r + 1] = make_float4((float)c3, (float)c5, (float)c6, (float)c7);
+  }
+}
+
+// Negative-value flags (CubeDev::negflag) from the padded scalar grid: node
+// (i, j, k) is flagged when a node of [i-1, i+2] x [j-1, j+2] x [k-1, k+2],
+// clamped to the grid, is below zero.
+__global__ void cube_negflag_kernel(const float* __restrict__ v, int nx, int ny, int nz, uint8_t* __restrict__ flag) {
+  const long long px = nx + 2, pxy = (long long)(nx + 2) * (ny + 2);
+  const long long n = (long long)nx * ny * nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % nx), j = (int)((t / nx) % ny), k = (int)(t / ((long long)nx * ny));
+    bool neg = false;
+    for (int kk = max(k - 1, 0); kk <= min(k + 2, nz - 1); ++kk)
+      for (int jj = max(j - 1, 0); jj <= min(j + 2, ny - 1); ++jj)
+        for (int ii = max(i - 1, 0); ii <= min(i + 2, nx - 1); ++ii)
+          neg |= v[(kk + 1) * pxy + (jj + 1) * px + (ii + 1)] < 0.f;
+    flag[t] = neg ? 1 : 0;
   }
 }
 
@@ -1219,6 +1357,13 @@ cudaError_t launch_cube_fill(const float*, int nx, int ny, int nz, float* dst, c
   long long total = 2ll * (nx + 2) * (ny + 2) + 2ll * (nx + 2) * nz + 2ll * ny * nz;
   int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
   cube_guard_kernel<<<blocks, 256, 0, s>>>(dst, nx, ny, nz);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cube_negflags(const float* padded, int nx, int ny, int nz, uint8_t* flags, cudaStream_t s) {
+  const long long n = (long long)nx * ny * nz;
+  int blocks = (int)std::min<long long>((n + 255) / 256, 8192);
+  cube_negflag_kernel<<<blocks, 256, 0, s>>>(padded, nx, ny, nz, flags);
   return cudaGetLastError();
 }
 

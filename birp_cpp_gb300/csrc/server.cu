@@ -40,6 +40,7 @@ struct Source {
   std::vector<double> ax[3];
   float* h_vals = nullptr;  // pinned host copy (cubes)
   int64_t bytes = 0;        // device bytes when resident
+  int has_neg = 0;          // a value below zero (the cube then carries flags)
   birp_cube* resident = nullptr;
   uint64_t last_use = 0;
   int in_use = 0;           // batches (forming or in flight) that reference it
@@ -144,6 +145,7 @@ void uploader_loop(birp_server* s) {
     if (rc == BIRP_OK) {
       birp_cube* c = new birp_cube();
       c->layout = s->cfg.cube_layout;
+      c->has_neg = src.has_neg;
       const int64_t reserved = src.bytes;
       s->resident_bytes += reserved;
       const float* vals = src.h_vals;
@@ -430,6 +432,7 @@ birp_status birp_server_add_cube(birp_server* s, const double* xs, int nx, const
   cudaError_t e = cudaHostAlloc(&src.h_vals, count * sizeof(float), cudaHostAllocDefault);
   if (e != cudaSuccess) return fail(BIRP_ERR_NOMEM, "pinned host copy: %s", cudaGetErrorString(e));
   std::memcpy(src.h_vals, values, count * sizeof(float));
+  src.has_neg = probe.has_neg = any_negative(src.h_vals, count) ? 1 : 0;
   src.bytes = (int64_t)cube_device_bytes(probe);
   std::lock_guard<std::mutex> lk(s->mu);
   s->sources.push_back(std::move(src));

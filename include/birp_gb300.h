@@ -117,8 +117,9 @@ typedef enum { BIRP_MARCH_PREFIX = 0, BIRP_MARCH_CLIP = 1 } birp_march;
  * explicit image dims (the reference uses round(fov / pixel_size_deg),
  * src/Camera.cpp:38-39), samples per ray (reference 200) and ray length in
  * Earth radii (reference 44): sample i sits at t = (i + 0.5) * ray_length /
- * n_samples. PREFIX stops a ray at its first out-of-box sample (the
- * reference, src/Camera.cpp:207); CLIP integrates every in-box sample.
+ * n_samples. PREFIX stops a ray at its first sample below zero: out of the
+ * box, or a negative cube value (the reference, src/Camera.cpp:205-209);
+ * CLIP skips such samples up to the first good one and stops at the next.
  * segments: lanes per ray (1, 2, 4, 8), 0 = tuned choice. */
 typedef struct {
   double pos[3];

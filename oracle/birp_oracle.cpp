@@ -12,7 +12,8 @@
 //    including its float/double promotions, its quirks (aim.y/aim.z ignored in
 //    the pose, the degrees/radians mix in Orient, the p2 bug in CMEM::Init, B
 //    overwritten by the field magnitude), the per-sample scale, serial FP32
-//    accumulation and stop-at-first-out-of-bounds. Generalised only by
+//    accumulation and the stop at the first sample < 0 (-1 out of bounds,
+//    or a negative field value). Generalised only by
 //    explicit image dims, sample count N and ray length L, plus an optional
 //    per-cell lookup for nonuniform axes. With reference inputs it matches the
 //    reference build (oracle/_ref) bit for bit; the tests check that.
@@ -20,8 +21,9 @@
 //  * "fp64": the FP64 oracle. The same physics in double precision, with the
 //    reference's float-typed inputs and constants promoted exactly, sample
 //    positions t_i = (i+0.5)*dt, a correct per-cell lookup on every axis,
-//    PREFIX (reference: stop at the first out-of-bounds sample) and CLIP
-//    (integrate every in-box sample) march modes. Its double-precision ray
+//    PREFIX (reference: stop at the first out-of-bounds or negative sample)
+//    and CLIP (skip such samples until the first good one, stop at the next)
+//    march modes. Its double-precision ray
 //    direction and in-box tests are written as plain IEEE +,-,*,/,sqrt with no
 //    contraction (build with -ffp-contract=off), so a GPU can reproduce them
 //    bit for bit; the scale factor is applied once per ray.
@@ -804,13 +806,17 @@ double render_pixel64(const Job64& J, int i, int j) {
         p[k] = J.f.pos[k] + d[k] * t;
         if (!in_axis64(ax[k], n[k], p[k])) in = false;
       }
-      if (!in) {
-        if (c->mode == 0) break;       // PREFIX: stop at the first out-of-bounds sample
-        if (started) break;            // CLIP: the in-box run is contiguous
+      // a negative value ends the run as an out-of-bounds sample does: the
+      // reference stops at the first scaled sample < 0 (src/Camera.cpp:205-209),
+      // its -1 outside the box and negative field values alike
+      const double v = in ? cube64_sample(cb, p) : -1.0;
+      if (v < 0.0) {  // (a NaN value is summed, as in the reference)
+        if (c->mode == 0) break;       // PREFIX: stop at the first bad sample
+        if (started) break;            // CLIP: the run ends at the first bad sample after it starts
         continue;
       }
       started = true;
-      sum += cube64_sample(cb, p);
+      sum += v;
     }
   } else {
     for (int s = 0; s < N; ++s) {

@@ -117,6 +117,20 @@ def main():
         meta.append(dict(key=f"img{k}", space="const", trilinear=0, pixel=3.0, fov_h=36.0, fov_w=36.0,
                          pos=(1.0, 1.0, 1.0), aim=(1.0, 0.0, 0.0), renders=renders))
         k += 1
+    # a signed field: the reference stops a ray at its first negative sample,
+    # not only at the box edge (own seed: the fixtures above are unchanged)
+    srng = np.random.default_rng(20261204)
+    vals_s = srng.uniform(-1.5, 5.0, size=vals.shape).astype(np.float32)
+    rd["values_signed"] = vals_s
+    for pos, aim in POSES[:3]:
+        for tri in (0, 1):
+            h = R.cube(xs, ys, zs, vals_s, tri)
+            img = R.render(h, 2.0, 36.0, 30.0, pos, aim)
+            R.free(h)
+            rd[f"img{k}"] = img
+            meta.append(dict(key=f"img{k}", space="cube_signed", trilinear=tri, pixel=2.0, fov_h=36.0,
+                             fov_w=30.0, pos=pos, aim=aim, renders=1))
+            k += 1
     np.savez_compressed(os.path.join(HERE, "renders.npz"), **rd)
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(dict(cmem_sets=CMEM_SETS, cmem_kats=CMEM_KATS, renders=meta,

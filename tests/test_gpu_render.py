@@ -250,21 +250,24 @@ def test_cube_sample_matches_oracle(birp, oracle, golden, cube1):
 
 
 def test_reference_golden_renders(birp, golden):
-    """The GPU render of the golden uniform cube with the reference's own
-    camera (200 samples over 44 Re, dims round(fov/pixel)) agrees with the
-    reference's FP32 images to FP32 accuracy."""
+    """The GPU render of the golden uniform cubes (one of them signed: rays end
+    at their first negative sample) with the reference's own camera (200
+    samples over 44 Re, dims round(fov/pixel)) agrees with the reference's
+    FP32 images to FP32 accuracy."""
     g = golden["renders"]
-    cube = birp.Cube(g["xs"].astype(np.float64), g["ys"].astype(np.float64), g["zs"].astype(np.float64), g["values"])
-    cm = birp.Cmem()
+    axes = (g["xs"].astype(np.float64), g["ys"].astype(np.float64), g["zs"].astype(np.float64))
+    spaces = {"cube": birp.Cube(*axes, g["values"]), "cube_signed": birp.Cube(*axes, g["values_signed"]),
+              "cmem_default": birp.Cmem()}
     for rec in golden["meta"]["renders"]:
         if rec["renders"] != 1 or rec["space"] == "const":
             continue
         want = g[rec["key"]]
         ny, nx = want.shape
         cam = birp.camera(rec["pos"], rec["aim"], rec["fov_w"], rec["fov_h"], nx, ny, trilinear=rec["trilinear"])
-        img = birp.render(cube if rec["space"] == "cube" else cm, cam)
+        img = birp.render(spaces[rec["space"]], cam)
         mx, rms, n = rel_err(img, want)
         assert mx < 3e-5, (rec["key"], mx)
+        assert np.array_equal(img == 0, want == 0), rec["key"]
 
 
 def test_linearity_full_size(birp, cube1):

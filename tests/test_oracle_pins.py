@@ -57,8 +57,9 @@ def test_cube_samples_bitwise(oracle, golden, tri):
 
 def _space32(oracle, golden, rec):
     g = golden["renders"]
-    if rec["space"] == "cube":
-        return oracle.Cube32(g["xs"], g["ys"], g["zs"], g["values"], rec["trilinear"], 0)
+    if rec["space"] in ("cube", "cube_signed"):
+        vals = g["values_signed"] if rec["space"] == "cube_signed" else g["values"]
+        return oracle.Cube32(g["xs"], g["ys"], g["zs"], vals, rec["trilinear"], 0)
     if rec["space"] == "cmem_default":
         return oracle.Cmem32()
     return oracle.Const()
@@ -81,7 +82,8 @@ def test_renders_bitwise(oracle, golden):
 
 def test_fp64_oracle_vs_reference(oracle, golden):
     """The FP64 oracle agrees with the reference's FP32 render to FP32
-    accuracy (the reference sums 200 FP32 samples serially)."""
+    accuracy (the reference sums 200 FP32 samples serially), including the
+    signed field whose rays end at their first negative sample."""
     g = golden["renders"]
     for rec in golden["meta"]["renders"]:
         if rec["renders"] != 1:
@@ -89,9 +91,10 @@ def test_fp64_oracle_vs_reference(oracle, golden):
         want = g[rec["key"]].astype(np.float64)
         ny, nx = want.shape
         cam = oracle.camera64(rec["pos"], rec["aim"], rec["fov_w"], rec["fov_h"], nx, ny)
-        if rec["space"] == "cube":
+        if rec["space"] in ("cube", "cube_signed"):
+            vals = g["values_signed"] if rec["space"] == "cube_signed" else g["values"]
             sp = oracle.Cube64(g["xs"].astype(np.float64), g["ys"].astype(np.float64), g["zs"].astype(np.float64),
-                               g["values"].astype(np.float64), rec["trilinear"])
+                               vals.astype(np.float64), rec["trilinear"])
         elif rec["space"] == "cmem_default":
             sp = oracle.Cmem64()
         else:
@@ -144,3 +147,40 @@ def test_prefix_equals_clip_inside_box(oracle):
     # the reference's config-0 pose lies outside the box: PREFIX renders zeros
     c = oracle.render64(cube, oracle.camera64((-2, -12, 16), (10, 0, 0), 27, 16, 24, 14, mode=oracle.PREFIX))
     assert not c.any()
+
+
+def test_negative_values_end_the_run(oracle):
+    """A negative field value ends a ray's run like the box edge does
+    (src/Camera.cpp:205-209): PREFIX stops at the first negative sample; CLIP
+    skips negative samples before its first good one and stops at the next.
+    Checked per sample against a march over the oracle's own point samples."""
+    xs = np.linspace(-3, 5, 9)
+    ys = np.linspace(-4, 4, 7)
+    zs = np.linspace(-2, 6, 5)
+    v = np.random.default_rng(8).uniform(-0.6, 2.0, (5, 7, 9))
+    for tri in (0, 1):
+        cube = oracle.Cube64(xs, ys, zs, v, tri)
+        for mode in (oracle.PREFIX, oracle.CLIP):
+            cam = oracle.camera64((0.5, 0.2, 1.0), (2.0, 0, 0), 70, 60, 9, 7, n_samples=300, ray_length=30.0,
+                                  mode=mode)
+            img = oracle.render64(cube, cam)
+            f = oracle.frame64(cam)
+            for j in range(7):
+                for i in range(9):
+                    d = oracle.ray_dir64(cam, i, j)
+                    t = (np.arange(300) + 0.5) * f["dt"]
+                    pts = np.asarray(cam.pos)[None, :] + t[:, None] * d[None, :]
+                    s = cube.sample(pts)  # -1 outside the box
+                    bad = s < 0
+                    if mode == oracle.PREFIX:
+                        end = int(np.argmax(bad)) if bad.any() else 300
+                        want = s[:end].sum()
+                    else:
+                        good = np.flatnonzero(~bad)
+                        if len(good) == 0:
+                            want = 0.0
+                        else:
+                            a = good[0]
+                            rest = np.flatnonzero(bad[a:])
+                            want = s[a:a + (rest[0] if len(rest) else 300 - a)].sum()
+                    assert np.isclose(img[j, i], want * f["K"], rtol=1e-12, atol=0), (tri, mode, i, j)
