@@ -9,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <mutex>
 #include <sstream>
 #include <stdexcept>
 #include <string>
@@ -29,15 +30,16 @@ void check(birp_status s) {
   throw std::runtime_error("birp: " + msg);
 }
 
-// The device is chosen once per process: BIRP_DEVICE (default 0).
+// The device is chosen once per process: BIRP_DEVICE (default 0). Safe to
+// call from several threads (a failed first attempt is retried by the next).
 void ensure_init() {
-  static bool done = false;
-  if (done) return;
-  const char* env = std::getenv("BIRP_DEVICE");
-  int dev = env ? std::atoi(env) : 0;
-  birp_status s = birp_init(dev);
-  if (s != BIRP_OK && s != BIRP_ERR_INVALID) check(s);
-  done = true;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const char* env = std::getenv("BIRP_DEVICE");
+    int dev = env ? std::atoi(env) : 0;
+    birp_status s = birp_init(dev);
+    if (s != BIRP_OK && s != BIRP_ERR_INVALID) check(s);  // throws: call_once runs again next time
+  });
 }
 
 }  // namespace

@@ -251,6 +251,13 @@ birp_status ensure_scratch(size_t img_floats) {
 
 birp_status check_init() {
   if (g_ctx.device < 0) return fail(BIRP_ERR_NOT_INIT, "birp_init has not been called");
+  // the current device is per host thread: a caller on another thread than
+  // birp_init's is switched to the library's device
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess || cur != g_ctx.device) {
+    const cudaError_t e = cudaSetDevice(g_ctx.device);
+    if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "cudaSetDevice(%d): %s", g_ctx.device, cudaGetErrorString(e));
+  }
   return BIRP_OK;
 }
 

@@ -128,6 +128,7 @@ birp_status make_room(birp_server* s, int id) {
 // Uploader thread: makes the queued cubes resident one at a time, with the
 // lock released during the upload itself, and wakes the scheduler.
 void uploader_loop(birp_server* s) {
+  cudaSetDevice(g_ctx.device);  // per host thread
   std::unique_lock<std::mutex> lk(s->mu);
   while (!s->stop) {
     if (s->upload_q.empty()) {
@@ -176,6 +177,7 @@ void uploader_loop(birp_server* s) {
 }
 
 void slot_worker(birp_server* s, Slot* slot) {
+  cudaSetDevice(g_ctx.device);  // per host thread
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
     slot->cv.wait(lk, [&] { return slot->has_work || s->stop; });
@@ -203,6 +205,7 @@ void slot_worker(birp_server* s, Slot* slot) {
 }
 
 void scheduler_loop(birp_server* s) {
+  cudaSetDevice(g_ctx.device);  // per host thread
   std::unique_lock<std::mutex> lk(s->mu);
   const auto window = std::chrono::duration<double, std::milli>(s->cfg.max_wait_ms);
   while (!s->stop) {

@@ -5,7 +5,9 @@
 #include <cmath>
 #include <cstdio>
 #include <fstream>
+#include <functional>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "birp/Camera.h"
@@ -153,12 +155,50 @@ static void camera_files_and_accumulation(const std::string& dir) {
   CHECK(mx > 0);
 }
 
+// Cameras on several threads sharing one read-only cube (the reference's
+// threading model: GetSample has no side effects): the same images as one
+// after another.
+static void concurrent_cameras() {
+  std::vector<double> xs, ys, zs;
+  for (int i = 0; i < 48; ++i) xs.push_back(-10 + 30.0 * i / 47);
+  for (int i = 0; i < 40; ++i) ys.push_back(-15 + 30.0 * i / 39);
+  for (int i = 0; i < 36; ++i) zs.push_back(-15 + 30.0 * i / 35);
+  std::vector<float> vals;
+  for (int k = 0; k < 36; ++k)
+    for (int j = 0; j < 40; ++j)
+      for (int i = 0; i < 48; ++i) vals.push_back(1.0f + 0.01f * ((i * 7 + j * 13 + k * 29) % 97));
+  DataCube cube;
+  cube.Init(xs, ys, zs, vals);
+  cube.SetTrilinear(true);
+  const int n = 8;
+  std::vector<std::vector<std::vector<float>>> seq(n), par(n);
+  auto render = [&cube](int k, std::vector<std::vector<float>>& out) {
+    Camera cam(cube, 20.f, 30.f, 40 + k, 30);
+    float px = -2.f + k, py = -12.f, pz = 14.f - k;
+    cam.SetPosition(px, py, pz);
+    cam.SetAim(10.f, 0.f, 0.f);
+    cam.SetMarchMode(1);
+    cam.Render();
+    out = cam.image;
+  };
+  for (int k = 0; k < n; ++k) render(k, seq[k]);
+  std::vector<std::thread> ts;
+  for (int k = 0; k < n; ++k) ts.emplace_back(render, k, std::ref(par[k]));
+  for (auto& t : ts) t.join();
+  for (int k = 0; k < n; ++k) CHECK(seq[k] == par[k]);
+  float mx = 0;
+  for (auto& row : seq[0])
+    for (float v : row) mx = std::fmax(mx, v);
+  CHECK(mx > 0);
+}
+
 int main(int argc, char** argv) {
   std::string dir = argc > 1 ? argv[1] : ".";
   cmem_basic();
   cmem_init_params();
   datacube(dir);
   camera_files_and_accumulation(dir);
+  concurrent_cameras();
   std::printf("%d failures\n", failures);
   return failures;
 }

@@ -306,6 +306,34 @@ def test_edge_cases(birp, oracle):
         birp.Cube(np.array([0.0]), xs, xs, np.zeros((2, 2, 1), np.float32))
 
 
+def test_concurrent_callers_share_a_cube(birp, cube1):
+    """Host threads rendering different views of one cube at once (the
+    reference's Cameras may share a read-only cube across threads) get the
+    same images, bit for bit, as the same calls one after another; so do two
+    batch objects used from two threads."""
+    import concurrent.futures as cf
+    from birp_cpp_gb300 import synth
+    reqs = synth.config2_requests(24, seed=9)
+    cams = [birp.camera(p, a, synth.FOV_W, synth.FOV_H, min(nx, 288), min(ny, 168), n_samples=synth.n_samples(s))
+            for p, a, nx, ny, s in reqs]
+    cube = cube1["gpu"]
+    seq = [birp.render(cube, c) for c in cams]
+    with cf.ThreadPoolExecutor(8) as ex:
+        par = list(ex.map(lambda c: birp.render(cube, c), cams))
+    for k, (a, b) in enumerate(zip(seq, par)):
+        assert np.array_equal(a, b), k
+    halves = [cams[:12], cams[12:]]
+    batches = [birp.Batch(12, sum(c.nx * c.ny for c in h)) for h in halves]
+    want = [b.render([(cube, c) for c in h]) for b, h in zip(batches, halves)]
+    with cf.ThreadPoolExecutor(2) as ex:
+        got = list(ex.map(lambda bh: bh[0].render([(cube, c) for c in bh[1]]), zip(batches, halves)))
+    for w, g in zip(want, got):
+        for a, b in zip(w, g):
+            assert np.array_equal(a, b)
+    for b in batches:
+        b.close()
+
+
 def test_kernel_stats_readable(birp):
     s = birp.kernel_stats(reset=True)
     assert set(s) == {"exact_range_rays", "exact_nearest", "exact_cmem", "items", "samples", "cells"}
