@@ -283,35 +283,44 @@ def cpu_sample(reqs, host, seconds: float, threads: int, seed: int = 7):
     """The reference's FP32 render arithmetic (oracle port, per-cell lookup on
     the stretched axes) over random pixels drawn uniformly from all pixels of
     all requests, until `seconds` of wall time; returns (images/s, pixels,
-    wall s). images/s = n_requests / (time per pixel * total pixels)."""
+    wall s). images/s = n_requests / (time per pixel * total pixels). The
+    requests of a round are spread over `threads` host threads, one oracle
+    call (one thread inside) per request: the library call releases the GIL,
+    and a round holds ~1000 pixels per thread, so every thread has work."""
+    import concurrent.futures as cf
+    from birp_cpp_gb300 import synth
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as O
     O.build()
     xs, ys, zs, v32 = host
     cube = O.Cube32(xs.astype(np.float32), ys.astype(np.float32), zs.astype(np.float32), v32, 1, 1)
+    cams = [O.camera32(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(step), ray_max=44)
+            for pos, aim, nx, ny, step in reqs]
     npx = np.array([nx * ny for _, _, nx, ny, _ in reqs], np.int64)
     total_px = int(npx.sum())
     cum = np.cumsum(npx)
     rng = np.random.default_rng(seed)
     done_px, t_used = 0, 0.0
-    chunk = 256 * max(1, threads)  # ~256 pixels per thread per round
+    chunk = 1024 * max(1, threads)
+
+    def job(args):
+        r, loc = args
+        nx = reqs[r][2]
+        O.render32_pixels(cube, cams[r], loc % nx, loc // nx, threads=1)
+
     t_start = time.perf_counter()
-    while t_used < seconds or done_px == 0:
-        flat = rng.integers(0, total_px, chunk)
-        which = np.searchsorted(cum, flat, side="right")
-        local = flat - np.concatenate([[0], cum[:-1]])[which]
-        t0 = time.perf_counter()
-        for r in np.unique(which):
-            sel = which == r
-            pos, aim, nx, ny, step = reqs[r]
-            from birp_cpp_gb300 import synth
-            cam = O.camera32(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(step),
-                             ray_max=44)
-            O.render32_pixels(cube, cam, local[sel] % nx, local[sel] // nx, threads=threads)
-        t_used += time.perf_counter() - t0
-        done_px += chunk
-        if time.perf_counter() - t_start > 4 * seconds + 30:
-            break
+    with cf.ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        while t_used < seconds or done_px == 0:
+            flat = rng.integers(0, total_px, chunk)
+            which = np.searchsorted(cum, flat, side="right")
+            local = flat - np.concatenate([[0], cum[:-1]])[which]
+            jobs = [(int(r), local[which == r]) for r in np.unique(which)]
+            t0 = time.perf_counter()
+            list(ex.map(job, jobs))
+            t_used += time.perf_counter() - t0
+            done_px += chunk
+            if time.perf_counter() - t_start > 4 * seconds + 30:
+                break
     per_px = t_used / done_px
     return len(reqs) / (per_px * total_px), done_px, t_used
 
