@@ -684,8 +684,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     // Sample counts are exact integers and the field is continuous across
     // cell faces, so a sample on a face may go to either cell. The walk is
     // confined to cells [-1, n-1] by the guard cells' infinite exit planes,
-    // so every load is in bounds by construction; the loop is also capped at
-    // (samples + cells + 4) steps.
+    // so every load is in bounds by construction. An iteration that sums
+    // samples advances u by at least one; the others (a plane passed between
+    // two samples) step an axis, and they are also capped at samples + cells
+    // + 4.
     const CubeDev& C = *R.cube;
     const int total = b - a;
     const int seglen = (total + S - 1) >> SEGL2;
@@ -694,11 +696,12 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     nsamp = count;
     // per axis: position step st, its reciprocal, position at the run's first
     // sample, the run's first position relative to the current cell's base
-    // node (xb), the exit index ex, the walk-table pointer and the record step
-    // (compact layout: the inverse width iw of the current cell and the
-    // pointer g to its lower corner node instead of the record pointer q)
+    // node (xb), the exit index ex (= plane * rst + nb, nb = -bs * rst: one
+    // FMA per step), the walk-table pointer and the record step (compact
+    // layout: the inverse width iw of the current cell and the pointer g to
+    // its lower corner node instead of the record pointer q)
     using WalkEntry = std::conditional_t<COMPACT, float4, float2>;
-    float st[3], rst[3], bs[3], xb[3], ex[3];
+    float st[3], rst[3], bs[3], xb[3], ex[3], nb[3];
     [[maybe_unused]] float iw[3];
     const WalkEntry* wt[3];
     int dstr[3];
@@ -725,7 +728,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         const WalkEntry e = __ldg(wt[k]);  // {base node, exit plane[, 1/width]}
         xb[k] = bs[k] - e.x;
         // exit index of the cell along this axis: bs + ex * st = exit plane
-        ex[k] = (e.y - bs[k]) * rst[k];
+        nb[k] = -bs[k] * rst[k];
+        ex[k] = fmaf(e.y, rst[k], nb[k]);
         if constexpr (COMPACT) {
           iw[k] = e.z;
           const int stride = (int)record_stride(C.gx, C.gxy, k);  // in nodes
@@ -746,7 +750,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       float u = 0.f;
       const int cap = count + C.ax[0].n + C.ax[1].n + C.ax[2].n + 4;
       int ncell = 0;
-      for (int guard = 0; u < ub && guard < cap; ++guard) {
+      int guard = 0;
+      while (u < ub) {
         float4 lo, hi;  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
         if constexpr (COMPACT) {
           // the cell's trilinear coefficients from its 8 corners, in local
@@ -782,13 +787,14 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           const float p1 = fmaf(gx, st[0], fmaf(gy, st[1], gz * st[2]));
           const float p2 = fmaf(hxy, DxDy, fmaf(hxz, DxDz, a1 * DyDz));
           const float p3 = hi.w * DxDyDz;
-          const float mm1 = m * (m - 1.f);
-          const float s1 = 0.5f * mm1;
-          const float s2 = mm1 * (2.f * m - 1.f) * (1.f / 6.f);
+          const float s1 = 0.5f * fmaf(m, m, -m);  // m (m - 1) / 2, exact
+          const float s2 = s1 * fmaf(m, 2.f / 3.f, -1.f / 3.f);
           const float s3 = s1 * s1;
           acc.add(fmaf(p3, s3, fmaf(p2, s2, fmaf(p1, s1, f0v * m))));
           u = nxt;
           ++ncell;
+        } else if (++guard > cap) {
+          break;
         }
         // step each axis whose exit index has been reached, once: a second
         // plane passed before the next sample is stepped in the next
@@ -802,7 +808,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
             ++wt[k];
             const WalkEntry e = __ldg(wt[k]);
             xb[k] = bs[k] - e.x;
-            ex[k] = (e.y - bs[k]) * rst[k];
+            ex[k] = fmaf(e.y, rst[k], nb[k]);
             if constexpr (COMPACT) {
               iw[k] = e.z;
               g += dstr[k];
@@ -946,11 +952,14 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
                                : reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, kc[0], kc[1], kc[2]);
       int u = 0;
       const int cap = count + C.ax[0].n + C.ax[1].n + C.ax[2].n + 4;
-      for (int guard = 0; u < count && guard < cap; ++guard) {
+      int guard = 0;  // iterations that sum nothing (see the trilinear walk)
+      while (u < count) {
         const int nxt = min(min(min(nxtc[0], nxtc[1]), nxtc[2]), count);
         if (nxt > u) {
           acc.add(__ldg(q) * (float)(nxt - u));
           u = nxt;
+        } else if (++guard > cap) {
+          break;
         }
         if (u >= count) break;  // the run is summed: no further steps
         // one step per axis and iteration, as in the trilinear walk
