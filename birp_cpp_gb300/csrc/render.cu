@@ -950,6 +950,12 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       // exist, because a walk stops at the sentinel planes
       const float* q = COMPACT ? C.grid + record_index(C.gx, C.gxy, kc[0], kc[1], kc[2])
                                : reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, kc[0], kc[1], kc[2]);
+      // the next planes as indices into the node table of all three axes
+      // (one allocation: axis k's nodes start at nodes_ff[k])
+      const float2* nbase = C.nodes_ff[0];
+      int ni[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) ni[k] = (int)(np[k] - nbase);
       int u = 0;
       const int cap = count + C.ax[0].n + C.ax[1].n + C.ax[2].n + 4;
       int guard = 0;  // iterations that sum nothing (see the trilinear walk)
@@ -962,15 +968,46 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           break;
         }
         if (u >= count) break;  // the run is summed: no further steps
-        // one step per axis and iteration, as in the trilinear walk
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          if (nxtc[k] <= u) {  // never past a sentinel plane (kNever)
-            q += dstr[k];
-            np[k] += (dstr[k] > 0) ? 1 : -1;
-            nxtc[k] = cross(k, np[k]) - first_c;
+        // step the axis whose plane comes first (its crossing is <= u here; an
+        // axis due at the same sample is stepped next iteration, which sums
+        // nothing): one crossing per iteration, its operands chosen by
+        // selects; an undecided FP32 crossing goes to the full computation
+        const int k = (nxtc[0] <= nxtc[1]) ? (nxtc[0] <= nxtc[2] ? 0 : 2) : (nxtc[1] <= nxtc[2] ? 1 : 2);
+        const int ds = k == 0 ? dstr[0] : (k == 1 ? dstr[1] : dstr[2]);
+        q += ds;
+        const int nk = (k == 0 ? ni[0] : (k == 1 ? ni[1] : ni[2])) + (ds > 0 ? 1 : -1);
+        ni[0] = k == 0 ? nk : ni[0];
+        ni[1] = k == 1 ? nk : ni[1];
+        ni[2] = k == 2 ? nk : ni[2];
+        const float2* nd = nbase + nk;
+        const float invh = k == 0 ? inv[0].hi : (k == 1 ? inv[1].hi : inv[2].hi);
+        const float Kh = k == 0 ? K[0].hi : (k == 1 ? K[1].hi : K[2].hi);
+        const float Ek = k == 0 ? E32[0] : (k == 1 ? E32[1] : E32[2]);
+        const float2 P = __ldg(nd);
+        const float u32 = fmaf(P.x, invh, -Kh);
+        int c;
+        if (!(u32 <= (float)N + 1.5f)) {
+          c = kNever;  // also NaN: a sentinel plane
+        } else if (u32 < -1.5f) {
+          c = 0;
+        } else {
+          const float m0 = rintf(u32);
+          const float d32u = u32 - m0;
+          if (fabsf(d32u) > Ek) {
+            const int i = max((int)m0 + (d32u > 0.f ? 1 : 0), 0);
+            c = i < N ? i : kNever;
+          } else if (k == 0) {
+            c = cross(0, nd);
+          } else if (k == 1) {
+            c = cross(1, nd);
+          } else {
+            c = cross(2, nd);
           }
         }
+        c -= first_c;
+        nxtc[0] = k == 0 ? c : nxtc[0];
+        nxtc[1] = k == 1 ? c : nxtc[1];
+        nxtc[2] = k == 2 ? c : nxtc[2];
       }
     }
     n_exact_nearest = n_fp64;
