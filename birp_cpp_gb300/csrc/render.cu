@@ -254,9 +254,50 @@ struct CmemDir {
   float r, theta, ct, st, cp, sp, b2;  // b2 = 2 / (1 + cos theta)
 };
 
+// One-instruction base-2 exponential and reciprocal square root (PTX
+// ex2.approx.ftz / rsqrt.approx.ftz: ~2 ulp, subnormal inputs and results
+// flushed to zero). The CMEM arguments are normal numbers, and an exponential
+// that would be subnormal only drops a term below 1e-38 of its sum.
+__device__ __forceinline__ float ex2_fast(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsqrt_fast(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// atan2(y, x) for y >= 0 (result in [0, pi]; not both 0). With a = min/max
+// of (|x|, y) in [0, 1], atan(a) = a P(a^2) with P of degree 8, fitted for
+// this function by iteratively reweighted least squares toward the minimax
+// absolute error on 4000 Chebyshev nodes of a^2 in [0, 1] (largest error
+// 8.4e-8 rad evaluated in FP32); then atan(y/|x|) = pi/2 - atan(|x|/y) when
+// y > |x|, and pi - atan(y/|x|) when x < 0. Error <= ~2.5e-7 rad with the
+// hardware-reciprocal division.
+__device__ __forceinline__ float atan2_pos(float y, float x) {
+  const float ax = fabsf(x);
+  const float a = __fdividef(fminf(ax, y), fmaxf(ax, y));
+  const float s = a * a;
+  float p = 0.00245668f;
+  p = fmaf(p, s, -0.01440118f);
+  p = fmaf(p, s, 0.03978092f);
+  p = fmaf(p, s, -0.07234829f);
+  p = fmaf(p, s, 0.10498931f);
+  p = fmaf(p, s, -0.14161225f);
+  p = fmaf(p, s, 0.19985907f);
+  p = fmaf(p, s, -0.33332598f);
+  p = fmaf(p, s, 0.9999999f);
+  float r = a * p;
+  if (y > ax) r = 1.57079637f - r;
+  if (x < 0.f) r = 3.14159274f - r;
+  return r;
+}
+
 // sqrt(x) for x >= 0 from the hardware reciprocal square root (a few ulp;
 // exact 0 at 0, where x * rsqrt(x) would be 0 * inf)
-__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.f ? x * rsqrt_fast(x) : 0.f; }
 
 __device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
   CmemDir d;
@@ -264,11 +305,11 @@ __device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
   const float ryz = sqrt_fast(ryz2);
   d.r = sqrt_fast(fmaf(x, x, ryz2));
   if (x != 0.f) {
-    d.theta = atan2f(ryz, x);
+    d.theta = atan2_pos(ryz, x);
     const float ir = __fdividef(1.f, d.r);
     d.ct = x * ir;
     d.st = ryz * ir;
-    d.b2 = x >= 0.f ? 2.f * d.r / (d.r + x) : 2.f * d.r * (d.r - x) / ryz2;
+    d.b2 = x >= 0.f ? __fdividef(2.f * d.r, d.r + x) : __fdividef(2.f * d.r * (d.r - x), ryz2);
   } else {
     d.theta = 0.f;
     d.ct = 1.f;
@@ -286,7 +327,7 @@ __device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
   return d;
 }
 
-__device__ __forceinline__ float pow_pos(float a, float b) { return exp2f(b * __log2f(a)); }
+__device__ __forceinline__ float pow_pos(float a, float b) { return ex2_fast(b * __log2f(a)); }
 
 constexpr float kLog2e = 1.4426950408889634f;
 
@@ -295,21 +336,21 @@ __device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d,
   const float ux = d.ct, uy = d.st * d.cp, uz = d.st * d.sp;
   float dn = ux * m.cos_tn + uz * m.sin_tn;
   float cnx = uy * m.sin_tn, cny = uz * m.cos_tn - ux * m.sin_tn, cnz = -uy * m.cos_tn;
-  float phi_n = atan2f(sqrt_fast(cnx * cnx + cny * cny + cnz * cnz), dn);
+  float phi_n = atan2_pos(sqrt_fast(cnx * cnx + cny * cny + cnz * cnz), dn);
   float ds = ux * m.cos_ts - uz * m.sin_ts;
   float csx = -uy * m.sin_ts, csy = uz * m.cos_ts + ux * m.sin_ts, csz = -uy * m.cos_ts;
-  float phi_s = atan2f(sqrt_fast(csx * csx + csy * csy + csz * csz), ds);
-  const float ch = rsqrtf(d.b2);  // cos(theta / 2); b2 >= 1
-  float base = ch + m.a5 * (2.f * d.st * d.ct) * (1.f - exp2f(-kLog2e * d.theta));
+  float phi_s = atan2_pos(sqrt_fast(csx * csx + csy * csy + csz * csz), ds);
+  const float ch = rsqrt_fast(d.b2);  // cos(theta / 2); b2 >= 1
+  float base = ch + m.a5 * (2.f * d.st * d.ct) * (1.f - ex2_fast(-kLog2e * d.theta));
   float f = pow_pos(base, m.p1 * (m.bc0 + m.bc1 * d.cp + m.bc3 * (d.sp * d.sp)));
-  float q = m.p2c * exp2f(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
-            m.p2c * exp2f(kLog2e * m.p3ds * pow_pos(phi_s, m.a21));
+  float q = m.p2c * ex2_fast(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
+            m.p2c * ex2_fast(kLog2e * m.p3ds * pow_pos(phi_s, m.a21));
   r_mp = m.p0r0 * f + q;
   const float lb = __log2f(d.b2);
-  float ry = m.bs * exp2f(m.ay * lb);
-  float rz = m.bs * exp2f(m.az * lb);
+  float ry = m.bs * ex2_fast(m.ay * lb);
+  float rz = m.bs * ex2_fast(m.az * lb);
   float a1 = rz * d.cp, a2 = ry * d.sp;
-  r_bs = (ry * rz) * rsqrtf(a1 * a1 + a2 * a2);  // cp^2 + sp^2 = 1: the sum is > 0
+  r_bs = (ry * rz) * rsqrt_fast(a1 * a1 + a2 * a2);  // cp^2 + sp^2 = 1: the sum is > 0
 }
 
 __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
@@ -321,16 +362,29 @@ __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, floa
   CmemEval out;
   float tol = fmaf(m.eps_rel, r + 5.f, perr);
   out.unsure = !(fabsf(r - (r_mp + half)) > tol) || !(fabsf(r - (r_bs + half)) > tol);
-  float h = 0.5f * d.theta;
-  float h4 = (h * h) * (h * h);
-  float sheath = m.A1 * exp2f(-kLog2e * m.B * h4) * pow_pos(r * 0.1f, -m.alpha - m.beta * (d.st * d.st));
-  float d10 = r * 0.1f;
-  float outer = __fdividef(m.A2, d10 * d10 * d10);
+  // the shell the sample is in, by the reference's branch chain (NaN radii
+  // fall through it as there); the sheath and outer emissivities are
+  // computed only where the shell uses them
+  const int shell = (r < r_mp - half)                        ? 0
+                    : (r >= r_mp - half && r <= r_mp + half) ? 1
+                    : (r > r_mp + half && r < r_bs - half)   ? 2
+                    : (r >= r_bs - half && r <= r_bs + half) ? 3
+                                                             : 4;
+  float sheath = 0.f, outer = 0.f;
+  if (shell >= 1 && shell <= 3) {
+    const float h = 0.5f * d.theta;
+    const float h4 = (h * h) * (h * h);
+    sheath = m.A1 * ex2_fast(-kLog2e * m.B * h4) * pow_pos(r * 0.1f, -m.alpha - m.beta * (d.st * d.st));
+  }
+  if (shell >= 3) {
+    const float d10 = r * 0.1f;
+    outer = __fdividef(m.A2, d10 * d10 * d10);
+  }
   float v;
-  if (r < r_mp - half) v = 0.f;
-  else if (r >= r_mp - half && r <= r_mp + half) v = lerp_f(0.f, sheath, (r - (r_mp - half)) / (r_mp + half));
-  else if (r > r_mp + half && r < r_bs - half) v = sheath;
-  else if (r >= r_bs - half && r <= r_bs + half) v = lerp_f(sheath, outer, (r - (r_bs - half)) / (r_bs + half));
+  if (shell == 0) v = 0.f;
+  else if (shell == 1) v = lerp_f(0.f, sheath, (r - (r_mp - half)) / (r_mp + half));
+  else if (shell == 2) v = sheath;
+  else if (shell == 3) v = lerp_f(sheath, outer, (r - (r_bs - half)) / (r_bs + half));
   else v = outer;
   out.v = v;
   return out;
