@@ -35,7 +35,10 @@ namespace {
 
 constexpr int kThreads = 128;
 #ifndef BIRP_WALK_MINB
-#define BIRP_WALK_MINB 8  // resident CTAs per SM of the cube-walk batch kernels
+#define BIRP_WALK_MINB 8  // resident CTAs per SM of the records-layout trilinear batch kernel
+#endif
+#ifndef BIRP_COMPACT_MINB
+#define BIRP_COMPACT_MINB 7  // ... of the compact-layout trilinear batch kernel (forms 8 corners per cell)
 #endif
 #ifndef BIRP_NEAREST_MINB
 #define BIRP_NEAREST_MINB 8  // resident CTAs per SM of the nearest-mode batch kernel
@@ -1149,6 +1152,7 @@ template <int CLS>
 __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
                                            : CLS == BATCH_CMEM         ? BIRP_CMEM_MINB
                                            : CLS == BATCH_CUBE_NEAREST ? BIRP_NEAREST_MINB
+                                           : CLS == BATCH_CUBE_TRI_COMPACT ? BIRP_COMPACT_MINB
                                                                        : BIRP_WALK_MINB)
     render_batch_kernel(BatchDev B) {
   __shared__ TileSmem sm;
