@@ -223,10 +223,14 @@ def run_c4(args, B):
                                    max_queue=1 << 16, cube_layout=layout))
     ids = []
     for i in range(args.c4_cubes):
-        base = bases[i % len(bases)]
-        noise = (1.0 + 0.3 * rng.uniform(-1, 1, base.shape).astype(np.float32))
-        ids.append(srv.add_cube(xs, ys, zs, base * noise))
-        del noise
+        # base * (1 + 0.3 U(-1, 1)), in FP32 and in place (256 cubes of 75 M
+        # nodes are generated in minutes)
+        v = rng.random(bases[0].shape, dtype=np.float32)
+        v *= np.float32(0.6)
+        v += np.float32(0.7)
+        v *= bases[i % len(bases)]
+        ids.append(srv.add_cube(xs, ys, zs, v))
+        del v
     zipf_w = 1.0 / np.arange(1, args.c4_cubes + 1) ** 1.1
     zipf_w /= zipf_w.sum()
     reqs = synth.config2_requests(8192, seed=44)
