@@ -519,6 +519,20 @@ def main():
                      "peak_source": "measured in-run: FP32 FMA loop and L2-resident read (birp_measure_peaks)",
                      "fp32_frac": cells_per_step * FLOP_PER_CELL / t_k / 1e12 / fp32_tflops,
                      "l2_frac": cells_per_step * BYTES_PER_CELL / t_k / 1e9 / l2_gbs})
+    # the kernel is bound by instruction issue: warp instructions per cell
+    # segment (ncu, profiles/) against one warp instruction per scheduler and
+    # cycle (4 per SM) at the SM clock sampled during the timed steps
+    wipc = profile_value("warp_instructions_per_cell")
+
+    def issue_roofline(sm_mhz):
+        if not wipc or not sm_mhz:
+            return None
+        import torch
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        ai, peak = wipc * cells_per_step / t_k, 4.0 * sms * sm_mhz * 1e6
+        return {"bound": "issue", "achieved": ai, "peak": peak, "unit": "warp-inst/s", "frac": ai / peak,
+                "note": f"{wipc:.3f} warp instructions per cell segment (ncu, 64-request launch); peak = 4 x "
+                        f"{sms} SMs x {sm_mhz:.0f} MHz (median SM clock of the timed steps)"}
     roofline_per_sample = roof(samples_per_step, FLOP_PER_SAMPLE, BYTES_PER_SAMPLE,
                                f"{samples_per_step:.4g} ray-samples/launch x {FLOP_PER_SAMPLE:.0f} flop, "
                                f"{BYTES_PER_SAMPLE:.0f} B (per-sample formulation; the kernel sums "
@@ -549,7 +563,8 @@ def main():
                               "sample": f"{px1} random pixels, {t1:.1f} s on 1 thread"}
 
     if rank == 0:
-        h2d = len(items) * 232  # request descriptors (RequestDev) per step
+        h2d = batch.upload_bytes()  # request descriptors and work tables, copied each step
+        clock_summary = clocks.summary()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -562,12 +577,14 @@ def main():
             "e2e_breakdown": e2e_breakdown,
             "serving": serving,
             "ray_samples_per_s": samples_per_step * world / (step_ms / 1000.0),
-            "roofline": roofline, "roofline_per_sample": roofline_per_sample, "roofline_hbm": roofline_hbm,
+            "roofline": roofline, "roofline_issue": issue_roofline(clock_summary.get("sm_mhz")),
+            "roofline_per_sample": roofline_per_sample,
+            "roofline_hbm": roofline_hbm,
             "cpu_baseline": cpu, "parity": parity,
             # each step replays one graph with four kernels: the CMEM, nearest
             # and compact-layout ones (no work here) and the records-layout
             # trilinear one
-            "gpu_launches": 4 * args.steps, "clocks": clocks.summary(),
+            "gpu_launches": 4 * args.steps, "clocks": clock_summary,
             "exact_fp64_rays_per_step": ks["exact_range_rays"] / args.steps,
             "samples_per_cell": (ks["samples"] / ks["cells"]) if ks.get("cells") else None,
         }
@@ -646,16 +663,21 @@ def serve_latency(B, W, rate: float, seconds: float, seed: int = 13):
             "load": "70% of the saturated batched rate, Poisson"}
 
 
-def traffic_from_profile():
-    """DRAM bytes per launch of the batched kernel from the committed ncu
-    summary (profiles/), if present."""
+def profile_value(key):
+    """One figure of the batched kernel from the committed ncu summary
+    (profiles/render_batch_kernel_traffic.json), or None."""
     p = os.path.join(ROOT, "profiles", "render_batch_kernel_traffic.json")
     if os.path.exists(p):
         try:
-            return json.load(open(p)).get("dram_bytes_per_launch")
+            return json.load(open(p)).get(key)
         except (OSError, ValueError):
             return None
     return None
+
+
+def traffic_from_profile():
+    """DRAM bytes per launch of the batched kernel (ncu), if recorded."""
+    return profile_value("dram_bytes_per_launch")
 
 
 if __name__ == "__main__":

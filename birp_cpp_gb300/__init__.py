@@ -110,6 +110,7 @@ def lib():
             "birp_batch_image": ([P, I], C.POINTER(C.c_float)),
             "birp_batch_render": ([P, P, I, P], I),
             "birp_batch_last_ms": ([P, P, P], I),
+            "birp_batch_upload_bytes": ([P, P], I),
             "birp_server_default_config": ([P], None),
             "birp_server_create": ([P, P], I),
             "birp_server_destroy": ([P], I),
@@ -334,6 +335,11 @@ class Batch:
         k, t = C.c_float(), C.c_float()
         check(lib().birp_batch_last_ms(self.h, C.byref(k), C.byref(t)))
         return k.value, t.value
+
+    def upload_bytes(self) -> int:
+        n = C.c_size_t()
+        check(lib().birp_batch_upload_bytes(self.h, C.byref(n)))
+        return n.value
 
     def close(self):
         if self.h:

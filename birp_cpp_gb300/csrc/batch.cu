@@ -226,6 +226,12 @@ birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, fl
   return ok();
 }
 
+birp_status birp_batch_upload_bytes(const birp_batch* b, size_t* bytes) {
+  if (!b || !bytes) return fail(BIRP_ERR_INVALID, "NULL argument");
+  *bytes = b->stage_bytes;  // the one host -> device copy of the graph
+  return ok();
+}
+
 birp_status birp_batch_last_ms(const birp_batch* b, float* kernel_ms, float* total_ms) {
   if (!b || b->pending) return fail(BIRP_ERR_INVALID, "no finished launch");
   float k = 0, t = 0;

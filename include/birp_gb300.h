@@ -208,6 +208,10 @@ birp_status birp_batch_render_noalloc(const birp_request* reqs, int n, float* co
  * graph: H2D of descriptors, kernel, D2H of the images). */
 birp_status birp_batch_last_ms(const birp_batch* b, float* kernel_ms, float* total_ms);
 
+/* Bytes each launch of the batch copies host -> device: its request
+ * descriptors and work tables (fixed by the batch's max_requests). */
+birp_status birp_batch_upload_bytes(const birp_batch* b, size_t* bytes);
+
 /* ---------------------------------------------------------------- serving */
 
 /* A continuous-batching server: requests are admitted as they arrive; a
