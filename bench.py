@@ -527,8 +527,11 @@ def main():
     def issue_roofline(sm_mhz):
         if not wipc or not sm_mhz:
             return None
-        import torch
-        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        try:
+            import torch
+            sms = torch.cuda.get_device_properties(0).multi_processor_count
+        except Exception as e:  # a reporting extra: never fails the run
+            return {"bound": "issue", "achieved": None, "error": str(e)[:120]}
         ai, peak = wipc * cells_per_step / t_k, 4.0 * sms * sm_mhz * 1e6
         return {"bound": "issue", "achieved": ai, "peak": peak, "unit": "warp-inst/s", "frac": ai / peak,
                 "note": f"{wipc:.3f} warp instructions per cell segment (ncu, 64-request launch); peak = 4 x "
