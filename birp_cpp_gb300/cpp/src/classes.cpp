@@ -3,6 +3,9 @@
 // exception types: std::invalid_argument for bad input
 // (src/DataCube.cpp:136), std::runtime_error for a singular pose
 // (src/Helper.cpp:243) and for device errors.
+#include <algorithm>
+#include <cerrno>
+#include <charconv>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -13,6 +16,8 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../../include/birp_gb300.h"
@@ -87,16 +92,99 @@ void DataCube::Init(const std::vector<double>& xs, const std::vector<double>& ys
   }
 }
 
+namespace {
+
+bool is_space(char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
+
+// One token's value as the reference reads it (Helper::explode_float ->
+// std::stof, src/Helper.cpp:25-38): its leading number, trailing characters
+// ignored; 1 if it holds no number (std::invalid_argument there), 2 if the
+// number is out of range (std::out_of_range there). std::from_chars reads the
+// plain decimal forms; strtof with errno (what std::stof uses) decides the
+// rest: a leading '+', hex, values that are zero, subnormal or beyond float.
+int token_value(const char* p, const char* tok_end, float& v) {
+  auto r = std::from_chars(p, tok_end, v);
+  if (r.ec == std::errc() && r.ptr != p && std::isnormal(v)) return 0;
+  errno = 0;
+  char* q = nullptr;
+  v = std::strtof(p, &q);
+  if (q == p) return 1;
+  return errno == ERANGE ? 2 : 0;
+}
+
+// Reads the first `count` white-space separated tokens of [p, end) into out
+// on up to 32 threads: chunks split at white space, tokens counted per chunk,
+// then each chunk parsed at its offset. Returns 0, or the token_value error
+// (also 1 when there are fewer than `count` tokens).
+int parse_tokens(const char* p, const char* end, size_t count, float* out) {
+  const size_t bytes = (size_t)(end - p);
+  unsigned T = std::min(32u, std::max(1u, std::thread::hardware_concurrency()));
+  if (bytes < ((size_t)1 << 22)) T = 1;
+  std::vector<const char*> cut(T + 1, end);
+  cut[0] = p;
+  for (unsigned t = 1; t < T; ++t) {
+    const char* c = p + bytes / T * t;
+    while (c < end && !is_space(*c)) ++c;  // a token stays in the chunk it starts in
+    cut[t] = std::max(c, cut[t - 1]);
+  }
+  std::vector<size_t> n(T, 0), off(T + 1, 0);
+  std::vector<int> err(T, 0);
+  auto run = [&](auto fn) {
+    std::vector<std::thread> ts;
+    for (unsigned t = 1; t < T; ++t) ts.emplace_back(fn, t);
+    fn(0u);
+    for (auto& th : ts) th.join();
+  };
+  run([&](unsigned t) {
+    size_t k = 0;
+    bool prev_space = true;
+    for (const char* c = cut[t]; c < cut[t + 1]; ++c) {
+      const bool s = is_space(*c);
+      k += (!s && prev_space);
+      prev_space = s;
+    }
+    n[t] = k;
+  });
+  for (unsigned t = 0; t < T; ++t) off[t + 1] = off[t] + n[t];
+  if (off[T] < count) return 1;
+  run([&](unsigned t) {
+    const char* c = cut[t];
+    for (size_t i = off[t]; i < std::min(off[t + 1], count); ++i) {
+      while (is_space(*c)) ++c;
+      const char* e = c;
+      while (e < cut[t + 1] && !is_space(*e)) ++e;
+      if (int r = token_value(c, e, out[i])) {
+        err[t] = r;
+        return;
+      }
+      c = e;
+    }
+  });
+  for (int e : err)
+    if (e) return e;
+  return 0;
+}
+
+void throw_token_error(int e) {
+  if (e == 2) throw std::out_of_range("Datacube value out of range.");
+  throw std::invalid_argument("Datacube is invalid, inaccessible, or malformed.");
+}
+
+}  // namespace
+
 // The exported-MHD text format read by the reference (src/DataCube.cpp:28-138):
 // line 10 holds the node counts "nx ny nz"; from line 11 come the x, y and z
 // node coordinates, then the values with x fastest (rows of x, ny rows per
-// slice, nz slices), whitespace-separated across any line breaks.
+// slice, nz slices): white-space separated tokens across any line breaks, each
+// read as the reference reads a token (std::stof of it). The values are
+// parsed on all host threads.
 void DataCube::Load(std::string filename, bool debug) {
-  std::ifstream f(filename, std::ios::binary);
+  std::ifstream f(filename, std::ios::binary | std::ios::ate);
   if (!f) throw std::invalid_argument("Datacube is invalid, inaccessible, or malformed.");
-  std::stringstream ss;
-  ss << f.rdbuf();
-  const std::string text = ss.str();
+  std::string text((size_t)f.tellg(), '\0');
+  f.seekg(0);
+  if (!f.read(&text[0], (std::streamsize)text.size()))
+    throw std::invalid_argument("Datacube is invalid, inaccessible, or malformed.");
   // locate line 10 and the start of line 11
   size_t pos = 0;
   for (int line = 1; line < 10 && pos != std::string::npos; ++line) {
@@ -117,20 +205,19 @@ void DataCube::Load(std::string filename, bool debug) {
   for (int k = 0; k < 3; ++k) {
     ax[k].resize(dims[k]);
     for (long i = 0; i < dims[k]; ++i) {
-      float v = std::strtof(p, &q);
-      if (q == p) throw std::invalid_argument("Datacube is invalid, inaccessible, or malformed.");
+      while (p < end && is_space(*p)) ++p;
+      const char* e = p;
+      while (e < end && !is_space(*e)) ++e;
+      float v;
+      if (p >= end) throw_token_error(1);
+      if (int r = token_value(p, e, v)) throw_token_error(r);
       ax[k][i] = v;  // the reference reads coordinates as float
-      p = q;
+      p = e;
     }
   }
   const size_t count = (size_t)dims[0] * dims[1] * dims[2];
   std::vector<float> vals(count);
-  for (size_t i = 0; i < count; ++i) {
-    float v = std::strtof(p, &q);
-    if (q == p || p >= end) throw std::invalid_argument("Datacube is invalid, inaccessible, or malformed.");
-    vals[i] = v;
-    p = q;
-  }
+  if (int r = parse_tokens(p, end, count, vals.data())) throw_token_error(r);
   Init(ax[0], ax[1], ax[2], vals);
   if (debug && size.z > 80 && size.y > 79 && size.x > 100) {
     // the reference's debug markers (src/DataCube.cpp:127-133)

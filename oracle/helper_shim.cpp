@@ -1,12 +1,14 @@
-// C entry points over a Helper implementation (test infrastructure), compiled
-// twice: into oracle/_ref/libbirp_ref.so against the reference's own Helper
-// (oracle/build_ref.sh, where the reference tree is present) and by
-// tests/test_helper_parity.py against birp_cpp_gb300's Helper, so the two
-// are compared on the same inputs through ctypes.
+// C entry points over a Helper and a DataCube implementation (test
+// infrastructure), compiled twice: into oracle/_ref/libbirp_ref.so against
+// the reference's own classes (oracle/build_ref.sh, where the reference tree
+// is present) and by tests/test_helper_parity.py and
+// tests/test_loader_parity.py against birp_cpp_gb300's, so the two are
+// compared on the same inputs through ctypes.
 #include <stdexcept>
 #include <string>
 #include <vector>
 
+#include "DataCube.h"
 #include "Helper.h"
 
 float DateToJulianDate(int year, int month, float day);
@@ -92,5 +94,44 @@ int h_explode_float(const char* s, char delim, float* out, int cap) {
   return (int)v.size();
 }
 int h_equal_distance(const float* steps, int n) { return Helper::EqualDistance(std::vector<float>(steps, steps + n)); }
+
+}  // extern "C"
+
+extern "C" {
+
+// DataCube::Load of `path` through this build's DataCube: 0 with dims, the
+// axes (x, y, z concatenated, at most axes_cap) and the x-fastest values (at
+// most cap) copied out; 1 std::invalid_argument, 2 std::out_of_range, 3 any
+// other exception, 4 too many values or slices not of the axes' shape.
+int h_cube_load(const char* path, int* dims, float* axes, int axes_cap, float* vals, long cap) {
+  try {
+    DataCube c;
+    c.Load(std::string(path), false);
+    const std::vector<float>* ax[3] = {&c.coords_x, &c.coords_y, &c.coords_z};
+    int o = 0;
+    for (int k = 0; k < 3; ++k) {
+      dims[k] = (int)ax[k]->size();
+      if (o + dims[k] > axes_cap) return 4;
+      for (float v : *ax[k]) axes[o++] = v;
+    }
+    const size_t nx = dims[0], ny = dims[1], nz = dims[2];
+    if ((long)(nx * ny * nz) > cap || c.slices.size() < nz) return 4;
+    size_t i = 0;
+    for (size_t k = 0; k < nz; ++k) {
+      if (c.slices[k].size() != ny) return 4;
+      for (size_t j = 0; j < ny; ++j) {
+        if (c.slices[k][j].size() != nx) return 4;
+        for (size_t x = 0; x < nx; ++x) vals[i++] = c.slices[k][j][x];
+      }
+    }
+    return 0;
+  } catch (const std::out_of_range&) {
+    return 2;
+  } catch (const std::invalid_argument&) {
+    return 1;
+  } catch (...) {
+    return 3;
+  }
+}
 
 }  // extern "C"

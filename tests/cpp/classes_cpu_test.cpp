@@ -1,7 +1,10 @@
 // The C++ drop-in classes' host-only parts: the .dat loader and the FITS
 // writer (no GPU is touched). argv[1] = output directory.
+#include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <fstream>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -9,9 +12,76 @@
 #include "birp/Cmem.h"
 #include "birp/DataCube.h"
 
+static void write_cube(const std::string& path, const std::string& dims_and_body) {
+  std::ofstream f(path);
+  f << "meta\n";
+  for (int i = 2; i < 10; ++i) f << "#\n";
+  f << dims_and_body;
+}
+
+// 0 if loading `body` succeeds, 1 on std::invalid_argument, 2 on std::out_of_range
+static int load_outcome(const std::string& dir, const std::string& body, DataCube& c) {
+  std::string path = dir + "/tok.dat";
+  write_cube(path, body);
+  try {
+    c.Load(path, false);
+  } catch (const std::out_of_range&) {
+    return 2;
+  } catch (const std::invalid_argument&) {
+    return 1;
+  }
+  return 0;
+}
+
+// Tokens read as the reference reads them (std::stof of each white-space
+// separated token): the leading number counts, trailing characters do not;
+// a token without a number is invalid, an out-of-range number out_of_range.
+static int loader_tokens(const std::string& dir) {
+  int fails = 0;
+  const std::string axes = "2 2 2\n0 1\n0 1\n0 1\n";
+  DataCube c;
+  fails += load_outcome(dir, axes + "+1.5 2.5abc 3e0 -4 nan inf 0x1p3 1.5E+00-2.5E+00\n", c) != 0;
+  fails += !(c.slices[0][0][0] == 1.5f && c.slices[0][0][1] == 2.5f && c.slices[0][1][0] == 3.f &&
+             c.slices[0][1][1] == -4.f && std::isnan(c.slices[1][0][0]) && std::isinf(c.slices[1][0][1]) &&
+             c.slices[1][1][0] == 8.f && c.slices[1][1][1] == 1.5f);
+  DataCube d1, d2, d3;
+  fails += load_outcome(dir, axes + "1 2 3 4 5 6 7 abc\n", d1) != 1;
+  fails += load_outcome(dir, axes + "1 2 3 4 5 6 7 1e400\n", d2) != 2;
+  fails += load_outcome(dir, axes + "1 2 3 4 5 6 7\n", d3) != 1;  // one value short
+  // the multi-threaded path (chunks split at white space): 2^21 values written
+  // with 9 significant digits read back exactly
+  {
+    const int n = 128;
+    std::string path = dir + "/big.dat";
+    std::ofstream f(path);
+    f << "meta\n";
+    for (int i = 2; i < 10; ++i) f << "#\n";
+    f << n << " " << n << " " << n << "\n";
+    for (int k = 0; k < 3; ++k) {
+      for (int i = 0; i < n; ++i) f << i << (i + 1 < n ? " " : "\n");
+    }
+    std::vector<float> want((size_t)n * n * n);
+    char buf[32];
+    for (size_t i = 0; i < want.size(); ++i) {
+      want[i] = (float)std::sin(0.001 * (double)i) * 1e3f + (float)(i % 7);
+      std::snprintf(buf, sizeof buf, "%.9g", want[i]);
+      f << buf << ((i % 128 == 127) ? "\n" : "  ");
+    }
+    f.close();
+    DataCube b;
+    b.Load(path, false);
+    size_t bad = 0, i = 0;
+    for (int z = 0; z < n; ++z)
+      for (int y = 0; y < n; ++y)
+        for (int x = 0; x < n; ++x, ++i) bad += std::memcmp(&b.slices[z][y][x], &want[i], 4) != 0;
+    fails += bad != 0;
+  }
+  return fails;
+}
+
 int main(int argc, char** argv) {
   std::string dir = argc > 1 ? argv[1] : ".";
-  int fails = 0;
+  int fails = loader_tokens(dir);
   // a cube in the reference's text format, values spread over ragged lines
   {
     std::ofstream f(dir + "/t.dat");
