@@ -530,7 +530,7 @@ def main():
             return None
         try:
             import torch
-            sms = torch.cuda.get_device_properties(0).multi_processor_count
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
         except Exception as e:  # a reporting extra: never fails the run
             return {"bound": "issue", "achieved": None, "error": str(e)[:120]}
         ai, peak = wipc * cells_per_step / t_k, 4.0 * sms * sm_mhz * 1e6
