@@ -971,6 +971,27 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         }
         return i < N ? i : kNever;
       };
+      // a crossing whose FP32 estimate was within its bound of an integer,
+      // for the axis k of the walk step (operands chosen by the caller):
+      // float-float, then the oracle's FP64 predicate within that bound
+      auto cross_ff = [&](int k, const float2* nd, FF invk, FF Kk, float cpk) -> int {
+        const float2 P = __ldg(nd);
+        const FF u = ff_add(ff_mul({P.x, P.y}, invk), {-Kk.hi, -Kk.lo});
+        const float n0 = rintf(u.hi);
+        const float dist = (u.hi - n0) + u.lo;
+        const float E = fmaf(1e-14f * cpk, fabsf(invk.hi), fmaf(3e-13f, (float)(N + 2), 1e-9f));
+        int i;
+        if (fabsf(dist) > E) {
+          i = max((int)n0 + (dist > 0.f ? 1 : 0), 0);
+        } else {
+          ++n_fp64;
+          const double c = C.ax[k].c64[nd - C.nodes_ff[k]];
+          const float uc = u.hi + u.lo;
+          i = exact_first_past_ray(sm.A[lx], sm.B[ly], k, R.pos[k], R.dt, c, invk.hi > 0.f,
+                                   max((int)floorf(uc - E) - 1, 0), min((int)ceilf(uc + E) + 2, N));
+        }
+        return i < N ? i : kNever;
+      };
       // the lane's first cell, exactly; then the next plane on each axis
       int nxtc[3], dstr[3];
 #pragma unroll
@@ -1053,12 +1074,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           if (fabsf(d32u) > Ek) {
             const int i = max((int)m0 + (d32u > 0.f ? 1 : 0), 0);
             c = i < N ? i : kNever;
-          } else if (k == 0) {
-            c = cross(0, nd);
-          } else if (k == 1) {
-            c = cross(1, nd);
           } else {
-            c = cross(2, nd);
+            const FF ik = {invh, k == 0 ? inv[0].lo : (k == 1 ? inv[1].lo : inv[2].lo)};
+            const FF kk2 = {Kh, k == 0 ? K[0].lo : (k == 1 ? K[1].lo : K[2].lo)};
+            c = cross_ff(k, nd, ik, kk2, k == 0 ? cp[0] : (k == 1 ? cp[1] : cp[2]));
           }
         }
         c -= first_c;
