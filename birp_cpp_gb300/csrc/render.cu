@@ -619,7 +619,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 #pragma unroll
     for (int r = 0; r < 3; ++r) w64[r] = __dadd_rn(sm.A[lx][r], sm.B[ly][r]);
     float w0 = (float)w64[0], w1 = (float)w64[1], w2 = (float)w64[2];
-    float inv = rsqrtf(w0 * w0 + w1 * w1 + w2 * w2);
+    // explicit FMAs: the same rounding in every build of every kernel
+    float inv = rsqrtf(fmaf(w0, w0, fmaf(w1, w1, w2 * w2)));
     d32[0] = w0 * inv;
     d32[1] = w1 * inv;
     d32[2] = w2 * inv;
@@ -660,21 +661,86 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       b = b_lo;
     }
     if (!certain && valid) {
-      need_d64();
       int s = 0, e = N;
+      bool used64 = false;
+      // the float-float tier pays off in the records trilinear kernel; in the
+      // others its registers cost more than the FP64 searches it saves
+      if constexpr (INTERP == TRILINEAR && AXES == AXES_DDA) {
+        // An axis the FP32 bound leaves undecided is decided in float-float:
+        // its interval ends are the first samples past the box's first and
+        // last planes, u = P / (d dt) - K as in the nearest walk, with that
+        // walk's error bound (which covers the oracle's own FP64 position
+        // rounding). Only an end within that bound of an integer takes the
+        // oracle's FP64 predicate (a bracketed search).
+        FF wf[3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        int sk, ek;
-        if (est[k].parallel || est[k].s_lo != est[k].s_hi || est[k].e_lo != est[k].e_hi) {
-          axis_range_exact(R.pos[k], d64[k], C.ax[k].c_first, C.ax[k].c_last, R.dt, N, est[k].s_lo,
-                           est[k].e_lo, sk, ek);
-        } else {
-          sk = est[k].s_lo;
-          ek = est[k].e_lo;
-          if (sk >= ek) { sk = N; ek = N; }
+        for (int r = 0; r < 3; ++r) {
+          const float h = (float)w64[r];
+          wf[r] = {h, (float)(w64[r] - (double)h)};
         }
-        s = max(s, sk);
-        e = min(e, ek);
+        const FF rs = ff_rsqrt(ff_add(ff_add(ff_mul(wf[0], wf[0]), ff_mul(wf[1], wf[1])), ff_mul(wf[2], wf[2])));
+        const FF dtf = {R.dt_hi, R.dt_lo};
+        // first sample in [0, N] past plane P (N: none); -1 when undecided
+        auto ff_first_past = [&](float2 P, FF invk, FF Kk, float cpk) -> int {
+          const FF u = ff_add(ff_mul({P.x, P.y}, invk), {-Kk.hi, -Kk.lo});
+          if (!(u.hi < (float)N + 2.f)) return u.hi > 0.f ? N : -1;  // beyond the ray (NaN: undecided)
+          if (u.hi < -2.f) return 0;
+          const float n0 = rintf(u.hi);
+          const float dist = (u.hi - n0) + u.lo;
+          const float E = fmaf(1e-14f * cpk, fabsf(invk.hi), fmaf(3e-13f, (float)(N + 2), 1e-9f));
+          if (!(fabsf(dist) > E)) return -1;
+          return min(max((int)n0 + (dist > 0.f ? 1 : 0), 0), N);
+        };
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          int sk = 0, ek = N;
+          bool decided = false;
+          if (!est[k].parallel && est[k].s_lo == est[k].s_hi && est[k].e_lo == est[k].e_hi) {
+            sk = est[k].s_lo;
+            ek = est[k].e_lo;
+            decided = true;
+          } else if (wf[k].hi != 0.f) {
+            const AxisDev& A = C.ax[k];
+            const FF invk = ff_recip(ff_mul(ff_mul(wf[k], rs), dtf));
+            const FF Kk = ff_add(ff_mul({R.pos_hi[k], R.pos_lo[k]}, invk), {0.5f, 0.f});
+            const float cpk = fmaxf(fabsf((float)A.c_first), fabsf((float)A.c_last)) + fabsf(R.pos32[k]);
+            const int il = ff_first_past(__ldg(C.nodes_ff[k]), invk, Kk, cpk);
+            const int ih = ff_first_past(__ldg(C.nodes_ff[k] + (A.n - 1)), invk, Kk, cpk);
+            if (il >= 0 && ih >= 0) {
+              // moving up the ray enters at the first plane, moving down at the last
+              sk = invk.hi > 0.f ? il : ih;
+              ek = invk.hi > 0.f ? ih : il;
+              decided = true;
+            }
+          }
+          if (decided) {
+            if (sk >= ek) { sk = N; ek = N; }
+          } else {
+            need_d64();
+            used64 = true;
+            axis_range_exact(R.pos[k], d64[k], C.ax[k].c_first, C.ax[k].c_last, R.dt, N, est[k].s_lo,
+                             est[k].e_lo, sk, ek);
+          }
+          s = max(s, sk);
+          e = min(e, ek);
+        }
+      } else {
+        need_d64();
+        used64 = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          int sk, ek;
+          if (est[k].parallel || est[k].s_lo != est[k].s_hi || est[k].e_lo != est[k].e_hi) {
+            axis_range_exact(R.pos[k], d64[k], C.ax[k].c_first, C.ax[k].c_last, R.dt, N, est[k].s_lo,
+                             est[k].e_lo, sk, ek);
+          } else {
+            sk = est[k].s_lo;
+            ek = est[k].e_lo;
+            if (sk >= ek) { sk = N; ek = N; }
+          }
+          s = max(s, sk);
+          e = min(e, ek);
+        }
       }
       if (R.mode == MARCH_PREFIX) {
         a = 0;
@@ -683,7 +749,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         a = s;
         b = e;
       }
-      n_exact = (threadIdx.x & ((1 << R.seg_log2) - 1)) == 0;  // once per ray
+      n_exact = used64 && (threadIdx.x & ((1 << R.seg_log2) - 1)) == 0;  // once per ray
     }
     if (b < a) b = a;
   }
