@@ -92,7 +92,7 @@ struct birp_server {
 
 namespace {
 
-void finish(birp_server* s, Req* r, birp_status status) {
+void finish(birp_server*, Req* r, birp_status status) {
   r->status = status;
   r->t_done = Clock::now();
   r->done = true;
