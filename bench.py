@@ -14,9 +14,13 @@ one pass over all 512 requests.
   serving    p50/p99 latency of the continuous-batching server at 70% of the
              saturated rate (Poisson arrivals)
   roofline   the batched kernel against the slower of its FP32 work and its
-             gathered bytes at the L2 read rate, both peaks measured in-run
+             gathered bytes at the L2 read rate, both peaks measured in-run;
+             roofline_issue: its warp instructions (per cell segment, from the
+             committed ncu capture) against the SM issue rate at the sampled
+             clock, the bound it actually runs into
   cpu_baseline  the reference's FP32 render arithmetic (oracle port) on all
-             host cores over a bounded random pixel sample of the same workload
+             host cores over a bounded random pixel sample of the same
+             workload, and on one core
 
 `--impl reference` times only that CPU implementation (bounded samples).
 Multi-GPU (torchrun): replicas, one per rank, barrier + max over ranks.
