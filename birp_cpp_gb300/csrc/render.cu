@@ -1129,11 +1129,11 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         const float Ek = k == 0 ? E32[0] : (k == 1 ? E32[1] : E32[2]);
         const float2 P = __ldg(nd);
         const float u32 = fmaf(P.x, invh, -Kh);
+        // (the next plane's crossing is never behind the current sample: the
+        // general branch covers u32 < -1.5 too, giving 0)
         int c;
         if (!(u32 <= (float)N + 1.5f)) {
           c = kNever;  // also NaN: a sentinel plane
-        } else if (u32 < -1.5f) {
-          c = 0;
         } else {
           const float m0 = rintf(u32);
           const float d32u = u32 - m0;
