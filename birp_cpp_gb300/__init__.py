@@ -12,7 +12,9 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "lib", "libbirp_gb300.so")
+# BIRP_LIB selects another build of the library (the bounds-checking
+# lib/libbirp_gb300_debug.so, say)
+LIB_PATH = os.environ.get("BIRP_LIB") or os.path.join(HERE, "lib", "libbirp_gb300.so")
 HEADER = os.path.join(HERE, "..", "include", "birp_gb300.h")
 
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_SINGULAR, ERR_NOT_INIT, ERR_TIMEOUT, ERR_BUSY, ERR_DEVICE = range(9)
@@ -111,6 +113,7 @@ def lib():
             "birp_batch_render": ([P, P, I, P], I),
             "birp_batch_last_ms": ([P, P, P], I),
             "birp_batch_upload_bytes": ([P, P], I),
+            "birp_debug_bounds": ([P, I], I),
             "birp_server_default_config": ([P], None),
             "birp_server_create": ([P, P], I),
             "birp_server_destroy": ([P], I),
@@ -415,3 +418,12 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def debug_bounds(reset: bool = True) -> int:
+    """First out-of-range table access recorded by the bounds-checking build
+    (code << 48 | index; 0 if none). Raises BirpError in other builds."""
+    st = C.c_ulonglong()
+    check(lib().birp_debug_bounds(C.byref(st), int(reset)))
+    return st.value
+

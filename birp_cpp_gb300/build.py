@@ -70,6 +70,26 @@ def build(verbose: bool = False) -> str:
 
 
 CLI = os.path.join(LIBDIR, "birp")
+DEBUG_LIB = os.path.join(LIBDIR, "libbirp_gb300_debug.so")
+
+
+def build_debug_bounds() -> str:
+    """The bounds-checking library lib/libbirp_gb300_debug.so: render.cu with
+    BIRP_DEBUG_BOUNDS (every table access of the kernels checked, the first
+    violation recorded for birp_debug_bounds), the other units as built."""
+    build()
+    out = os.path.join(OBJ, "render_debug_bounds.o")
+    src = os.path.join(CSRC, "render.cu")
+    cmd = [nvcc()] + _flags() + ["-DBIRP_DEBUG_BOUNDS", "-c", src, "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    objs = [out] + [os.path.join(OBJ, os.path.splitext(s)[0] + ".o") for s in SOURCES if s != "render.cu"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", DEBUG_LIB] + objs + ["-lpthread"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return DEBUG_LIB
 
 
 def build_cli() -> str:

@@ -81,6 +81,13 @@ struct CubeDev {
   const uint8_t* negflag;
   float neg_cmax, neg_inv_gap;
   int neg_nmax;
+  // extents of the tables above, for the bounds-checking build
+  // (BIRP_DEBUG_BOUNDS): float4 of rec, floats of grid, entries of the walk
+  // table allocation, entries of nodes_ff (sentinels included), LUT bins,
+  // negflag bytes
+  long long rec_f4, grid_n;
+  int walk_n, nodes_n, lut_total;
+  long long neg_n;
 };
 
 // CMEM coefficients (src/Cmem.cpp:38-115 after Init), FP32 and FP64 copies.
@@ -166,6 +173,9 @@ cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
 cudaError_t launch_cube_negflags(const float* padded, int nx, int ny, int nz, uint8_t* flags, cudaStream_t stream);
+// bounds-checking build: the first out-of-range access (code << 48 | index),
+// 0 if none, optionally reset; other builds: always 0, returns false
+bool read_bounds_status(unsigned long long* status, bool reset);
 cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, const double* cx64, const double* cy64,
                                 const double* cz64, float4* rec, cudaStream_t stream);
 cudaError_t launch_cube_sample(const CubeDev* cube, int trilinear, const float* xyz, int n, float* out,

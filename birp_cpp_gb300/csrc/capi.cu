@@ -625,6 +625,17 @@ birp_status birp_time_render_device(const birp_cube* cube, const birp_cmem* cmem
   return ok();
 }
 
+birp_status birp_debug_bounds(unsigned long long* status, int reset) {
+  if (birp_status s = check_init()) return s;
+  if (!status) return fail(BIRP_ERR_INVALID, "NULL argument");
+  CK(cudaDeviceSynchronize());
+  if (!read_bounds_status(status, reset != 0)) {
+    *status = 0;
+    return fail(BIRP_ERR_INVALID, "not a bounds-checking build (BIRP_DEBUG_BOUNDS)");
+  }
+  return ok();
+}
+
 birp_status birp_get_kernel_stats(birp_kernel_stats* out, int reset) {
   if (birp_status s = check_init()) return s;
   if (!out) return fail(BIRP_ERR_INVALID, "NULL argument");

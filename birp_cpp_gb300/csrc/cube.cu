@@ -276,6 +276,12 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     off += a.n;
   }
   d.negflag = c.d_negflag;
+  d.rec_f4 = compact ? 0 : (long long)(records * 2);
+  d.grid_n = compact ? (long long)total : 0;
+  d.walk_n = (int)walk.size();
+  d.nodes_n = (int)nodes_ff.size();
+  d.lut_total = (int)lut.size();
+  d.neg_n = c.has_neg ? (long long)nodes : 0;
   if (c.has_neg) {
     double cmax = 0.0, inv_gap = 0.0;
     for (int k = 0; k < 3; ++k) {

@@ -48,6 +48,18 @@ constexpr int kThreads = 128;
 #endif
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
+
+#ifdef BIRP_DEBUG_BOUNDS
+// Bounds-checking build: the first out-of-range table access of any kernel
+// (code << 48 | index); the caller then redirects the access to a valid
+// element, so a violation is reported, never a fault.
+__device__ unsigned long long g_bounds_status;
+__device__ __forceinline__ bool bound_ok(long long i, long long n, unsigned long long code) {
+  if (i >= 0 && i < n) return true;
+  atomicCAS(&g_bounds_status, 0ull, (code << 48) | ((unsigned long long)i & 0xffffffffffffull));
+  return false;
+}
+#endif
 // Bound on |d32 - d64| per component of the unit ray direction. d32 is the
 // FP64 w rounded to FP32 (0.5 ulp), |w|^2 in FP32 (<= 3 ulp with the input
 // rounding), rsqrtf (<= 2 ulp) and one multiply: <= 9 * 2^-24 = 5.4e-7.
@@ -438,7 +450,11 @@ __device__ __forceinline__ float lut_index(const AxisDev& a, const float4* __res
   float fb = fminf(fmaxf((x - a.lut_x0) * a.lut_inv_w, 0.f), (float)(a.lut_n - 1));
   int bits;
   magic_floor(fb, bits);
-  float4 e = __ldg(lut + a.lut_off + (bits - kMagicBits));
+  int bin = bits - kMagicBits;
+#ifdef BIRP_DEBUG_BOUNDS
+  if (!bound_ok(bin, a.lut_n, 1)) bin = 0;
+#endif
+  float4 e = __ldg(lut + a.lut_off + bin);
   float dx = x - e.x;
   return fmaf(dx, dx < 0.f ? e.z : e.w, e.y);
 }
@@ -493,8 +509,11 @@ __device__ __forceinline__ double lerp64(double a, double b, double t) {
 // Node (i, j, k)'s input value in either layout: the padded grid, or c0 of
 // the record of the cell whose lower corner it is (exactly the FP32 input).
 __device__ __forceinline__ double node_value(const CubeDev& C, int i, int j, int k) {
-  return C.compact ? (double)__ldg(C.grid + record_index(C.gx, C.gxy, i, j, k))
-                   : (double)__ldg(reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, i, j, k));
+  long long o = C.compact ? record_index(C.gx, C.gxy, i, j, k) : 8 * record_index(C.cx, C.cxy, i, j, k);
+#ifdef BIRP_DEBUG_BOUNDS
+  if (!bound_ok(o, C.compact ? C.grid_n : 4 * C.rec_f4, 2)) o = 0;
+#endif
+  return C.compact ? (double)__ldg(C.grid + o) : (double)__ldg(reinterpret_cast<const float*>(C.rec) + o);
 }
 
 // Whether in-box sample i of a ray is below zero in the FP64 oracle's own
@@ -558,7 +577,11 @@ __device__ __forceinline__ int neg_search(const RequestDev* Rp, float d0, float 
         g[k] = kb - kMagicBits;
       }
       bool neg = false;
-      if (all_exact || __ldg(C.negflag + ((size_t)g[2] * C.ax[1].n + g[1]) * C.ax[0].n + g[0]))
+      long long fi = ((long long)g[2] * C.ax[1].n + g[1]) * C.ax[0].n + g[0];
+#ifdef BIRP_DEBUG_BOUNDS
+      if (!bound_ok(fi, C.neg_n, 3)) fi = 0;
+#endif
+      if (all_exact || __ldg(C.negflag + fi))
         neg = sample_negative64(R.cube, R.interp, a, b, R.pos[0], R.pos[1], R.pos[2], R.dt, i, g[0], g[1], g[2]);
       hit = neg == want_neg;
     }
@@ -704,8 +727,14 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
             const FF invk = ff_recip(ff_mul(ff_mul(wf[k], rs), dtf));
             const FF Kk = ff_add(ff_mul({R.pos_hi[k], R.pos_lo[k]}, invk), {0.5f, 0.f});
             const float cpk = fmaxf(fabsf((float)A.c_first), fabsf((float)A.c_last)) + fabsf(R.pos32[k]);
-            const int il = ff_first_past(__ldg(C.nodes_ff[k]), invk, Kk, cpk);
-            const int ih = ff_first_past(__ldg(C.nodes_ff[k] + (A.n - 1)), invk, Kk, cpk);
+            const float2* pl = C.nodes_ff[k];
+            const float2* ph = C.nodes_ff[k] + (A.n - 1);
+#ifdef BIRP_DEBUG_BOUNDS
+            if (!bound_ok(pl - (C.nodes_ff[0] - 1), C.nodes_n, 4)) pl = C.nodes_ff[0];
+            if (!bound_ok(ph - (C.nodes_ff[0] - 1), C.nodes_n, 4)) ph = C.nodes_ff[0];
+#endif
+            const int il = ff_first_past(__ldg(pl), invk, Kk, cpk);
+            const int ih = ff_first_past(__ldg(ph), invk, Kk, cpk);
             if (il >= 0 && ih >= 0) {
               // moving up the ray enters at the first plane, moving down at the last
               sk = invk.hi > 0.f ? il : ih;
@@ -848,6 +877,12 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         const bool up = !signbit(d32[k]);
         if constexpr (COMPACT) wt[k] = up ? C.walk4_up[k] + k0s[k] : C.walk4_dn[k] - k0s[k];
         else wt[k] = up ? C.walk_up[k] + k0s[k] : C.walk_dn[k] - k0s[k];
+#ifdef BIRP_DEBUG_BOUNDS
+        {
+          const WalkEntry* wb = (COMPACT ? (const WalkEntry*)C.walk4_up[0] : (const WalkEntry*)C.walk_up[0]) - 1;
+          if (!bound_ok(wt[k] - wb, C.walk_n, 5)) wt[k] = wb;
+        }
+#endif
         const WalkEntry e = __ldg(wt[k]);  // {base node, exit plane[, 1/width]}
         xb[k] = bs[k] - e.x;
         // exit index of the cell along this axis: bs + ex * st = exit plane
@@ -879,6 +914,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         if constexpr (COMPACT) {
           // the cell's trilinear coefficients from its 8 corners, in local
           // physical coordinates (scaled by the inverse widths)
+#ifdef BIRP_DEBUG_BOUNDS
+          if (!bound_ok(g - C.grid, C.grid_n - (gxy + gx + 1), 7)) g = C.grid;
+#endif
           const float v000 = __ldg(g), v001 = __ldg(g + 1), v010 = __ldg(g + gx), v011 = __ldg(g + gx + 1);
           const float v100 = __ldg(g + gxy), v101 = __ldg(g + gxy + 1), v110 = __ldg(g + gxy + gx),
                       v111 = __ldg(g + gxy + gx + 1);
@@ -890,6 +928,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           lo = make_float4(v000, d1 * iw[0], d2 * iw[1], e4 * ixy);
           hi = make_float4(d3 * iw[2], e5 * (iw[0] * iw[2]), e6 * (iw[1] * iw[2]), e7 * (ixy * iw[2]));
         } else {
+#ifdef BIRP_DEBUG_BOUNDS
+          if (!bound_ok(q - C.rec, C.rec_f4 - 1, 6)) q = C.rec;
+#endif
           lo = __ldg(q);
           hi = __ldg(q + 1);
         }
@@ -929,6 +970,12 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         for (int k = 0; k < 3; ++k) {
           if (ex[k] <= u) {
             ++wt[k];
+#ifdef BIRP_DEBUG_BOUNDS
+            {
+              const WalkEntry* wb = (COMPACT ? (const WalkEntry*)C.walk4_up[0] : (const WalkEntry*)C.walk_up[0]) - 1;
+              if (!bound_ok(wt[k] - wb, C.walk_n, 5)) wt[k] = wb;
+            }
+#endif
             const WalkEntry e = __ldg(wt[k]);
             xb[k] = bs[k] - e.x;
             ex[k] = fmaf(e.y, rst[k], nb[k]);
@@ -1005,6 +1052,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       // a sentinel
       constexpr int kNever = 0x3fffffff;
       auto cross = [&](int k, const float2* nd) -> int {
+#ifdef BIRP_DEBUG_BOUNDS
+        if (!bound_ok(nd - (C.nodes_ff[0] - 1), C.nodes_n, 8)) nd = C.nodes_ff[0];
+#endif
         const float2 P = __ldg(nd);
         // FP32 estimate first; float-float only within its bound of an integer
         const float u32 = fmaf(P.x, inv[k].hi, -K[k].hi);
@@ -1030,7 +1080,11 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         } else {
           // within the bound: the oracle's predicate decides
           ++n_fp64;
-          const double c = C.ax[k].c64[nd - C.nodes_ff[k]];
+          long long ci = nd - C.nodes_ff[k];
+#ifdef BIRP_DEBUG_BOUNDS
+          if (!bound_ok(ci, C.ax[k].n, 8)) ci = 0;
+#endif
+          const double c = C.ax[k].c64[ci];
           const float uc = u.hi + u.lo;
           i = exact_first_past_ray(sm.A[lx], sm.B[ly], k, R.pos[k], R.dt, c, inv[k].hi > 0.f,
                                    max((int)floorf(uc - E) - 1, 0), min((int)ceilf(uc + E) + 2, N));
@@ -1041,6 +1095,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       // for the axis k of the walk step (operands chosen by the caller):
       // float-float, then the oracle's FP64 predicate within that bound
       auto cross_ff = [&](int k, const float2* nd, FF invk, FF Kk, float cpk) -> int {
+#ifdef BIRP_DEBUG_BOUNDS
+        if (!bound_ok(nd - (C.nodes_ff[0] - 1), C.nodes_n, 8)) nd = C.nodes_ff[0];
+#endif
         const float2 P = __ldg(nd);
         const FF u = ff_add(ff_mul({P.x, P.y}, invk), {-Kk.hi, -Kk.lo});
         const float n0 = rintf(u.hi);
@@ -1051,7 +1108,11 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           i = max((int)n0 + (dist > 0.f ? 1 : 0), 0);
         } else {
           ++n_fp64;
-          const double c = C.ax[k].c64[nd - C.nodes_ff[k]];
+          long long ci = nd - C.nodes_ff[k];
+#ifdef BIRP_DEBUG_BOUNDS
+          if (!bound_ok(ci, C.ax[k].n, 8)) ci = 0;
+#endif
+          const double c = C.ax[k].c64[ci];
           const float uc = u.hi + u.lo;
           i = exact_first_past_ray(sm.A[lx], sm.B[ly], k, R.pos[k], R.dt, c, invk.hi > 0.f,
                                    max((int)floorf(uc - E) - 1, 0), min((int)ceilf(uc + E) + 2, N));
@@ -1106,6 +1167,12 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       while (u < count) {
         const int nxt = min(min(min(nxtc[0], nxtc[1]), nxtc[2]), count);
         if (nxt > u) {
+#ifdef BIRP_DEBUG_BOUNDS
+          {
+            const float* vb = COMPACT ? C.grid : reinterpret_cast<const float*>(C.rec);
+            if (!bound_ok(q - vb, COMPACT ? C.grid_n : 4 * C.rec_f4, 9)) q = vb;
+          }
+#endif
           acc.add(__ldg(q) * (float)(nxt - u));
           u = nxt;
         } else if (++guard > cap) {
@@ -1127,6 +1194,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         const float invh = k == 0 ? inv[0].hi : (k == 1 ? inv[1].hi : inv[2].hi);
         const float Kh = k == 0 ? K[0].hi : (k == 1 ? K[1].hi : K[2].hi);
         const float Ek = k == 0 ? E32[0] : (k == 1 ? E32[1] : E32[2]);
+#ifdef BIRP_DEBUG_BOUNDS
+        if (!bound_ok(nd - (C.nodes_ff[0] - 1), C.nodes_n, 8)) nd = C.nodes_ff[0];
+#endif
         const float2 P = __ldg(nd);
         const float u32 = fmaf(P.x, invh, -Kh);
         // (the next plane's crossing is never behind the current sample: the
@@ -1545,6 +1615,21 @@ cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int
   else if (cls == BATCH_CUBE_NEAREST) render_batch_kernel<BATCH_CUBE_NEAREST><<<grid, kThreads, 0, s>>>(b);
   else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b);
   return cudaGetLastError();
+}
+
+bool read_bounds_status(unsigned long long* status, bool reset) {
+#ifdef BIRP_DEBUG_BOUNDS
+  if (cudaMemcpyFromSymbol(status, g_bounds_status, sizeof *status) != cudaSuccess) return false;
+  if (reset) {
+    const unsigned long long zero = 0;
+    if (cudaMemcpyToSymbol(g_bounds_status, &zero, sizeof zero) != cudaSuccess) return false;
+  }
+  return true;
+#else
+  *status = 0;
+  (void)reset;
+  return false;
+#endif
 }
 
 cudaError_t launch_cube_fill(const float*, int nx, int ny, int nz, float* dst, cudaStream_t s) {

@@ -212,6 +212,15 @@ birp_status birp_batch_last_ms(const birp_batch* b, float* kernel_ms, float* tot
  * descriptors and work tables (fixed by the batch's max_requests). */
 birp_status birp_batch_upload_bytes(const birp_batch* b, size_t* bytes);
 
+/* The library built with BIRP_DEBUG_BOUNDS (libbirp_gb300_debug.so) checks
+ * every table access of the render kernels; the first out-of-range one is
+ * recorded (code << 48 | index; codes: 1 index table, 2 node value, 3
+ * negative-value flag, 4 box plane, 5 walk table, 6 cell record, 7 padded
+ * grid, 8 node plane, 9 nearest value) and redirected to a valid element.
+ * Gives that status (0: none) and resets it when `reset`; in other builds
+ * *status = 0 and BIRP_ERR_INVALID. No counterpart in the reference. */
+birp_status birp_debug_bounds(unsigned long long* status, int reset);
+
 /* ---------------------------------------------------------------- serving */
 
 /* A continuous-batching server: requests are admitted as they arrive; a
