@@ -450,11 +450,13 @@ __device__ __forceinline__ float lut_index(const AxisDev& a, const float4* __res
   float fb = fminf(fmaxf((x - a.lut_x0) * a.lut_inv_w, 0.f), (float)(a.lut_n - 1));
   int bits;
   magic_floor(fb, bits);
-  int bin = bits - kMagicBits;
 #ifdef BIRP_DEBUG_BOUNDS
+  int bin = bits - kMagicBits;
   if (!bound_ok(bin, a.lut_n, 1)) bin = 0;
-#endif
   float4 e = __ldg(lut + a.lut_off + bin);
+#else
+  float4 e = __ldg(lut + a.lut_off + (bits - kMagicBits));
+#endif
   float dx = x - e.x;
   return fmaf(dx, dx < 0.f ? e.z : e.w, e.y);
 }
@@ -509,11 +511,14 @@ __device__ __forceinline__ double lerp64(double a, double b, double t) {
 // Node (i, j, k)'s input value in either layout: the padded grid, or c0 of
 // the record of the cell whose lower corner it is (exactly the FP32 input).
 __device__ __forceinline__ double node_value(const CubeDev& C, int i, int j, int k) {
-  long long o = C.compact ? record_index(C.gx, C.gxy, i, j, k) : 8 * record_index(C.cx, C.cxy, i, j, k);
 #ifdef BIRP_DEBUG_BOUNDS
+  long long o = C.compact ? record_index(C.gx, C.gxy, i, j, k) : 8 * record_index(C.cx, C.cxy, i, j, k);
   if (!bound_ok(o, C.compact ? C.grid_n : 4 * C.rec_f4, 2)) o = 0;
-#endif
   return C.compact ? (double)__ldg(C.grid + o) : (double)__ldg(reinterpret_cast<const float*>(C.rec) + o);
+#else
+  return C.compact ? (double)__ldg(C.grid + record_index(C.gx, C.gxy, i, j, k))
+                   : (double)__ldg(reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, i, j, k));
+#endif
 }
 
 // Whether in-box sample i of a ray is below zero in the FP64 oracle's own
@@ -577,11 +582,13 @@ __device__ __forceinline__ int neg_search(const RequestDev* Rp, float d0, float 
         g[k] = kb - kMagicBits;
       }
       bool neg = false;
-      long long fi = ((long long)g[2] * C.ax[1].n + g[1]) * C.ax[0].n + g[0];
 #ifdef BIRP_DEBUG_BOUNDS
+      long long fi = ((long long)g[2] * C.ax[1].n + g[1]) * C.ax[0].n + g[0];
       if (!bound_ok(fi, C.neg_n, 3)) fi = 0;
-#endif
       if (all_exact || __ldg(C.negflag + fi))
+#else
+      if (all_exact || __ldg(C.negflag + ((size_t)g[2] * C.ax[1].n + g[1]) * C.ax[0].n + g[0]))
+#endif
         neg = sample_negative64(R.cube, R.interp, a, b, R.pos[0], R.pos[1], R.pos[2], R.dt, i, g[0], g[1], g[2]);
       hit = neg == want_neg;
     }
@@ -727,14 +734,17 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
             const FF invk = ff_recip(ff_mul(ff_mul(wf[k], rs), dtf));
             const FF Kk = ff_add(ff_mul({R.pos_hi[k], R.pos_lo[k]}, invk), {0.5f, 0.f});
             const float cpk = fmaxf(fabsf((float)A.c_first), fabsf((float)A.c_last)) + fabsf(R.pos32[k]);
+#ifdef BIRP_DEBUG_BOUNDS
             const float2* pl = C.nodes_ff[k];
             const float2* ph = C.nodes_ff[k] + (A.n - 1);
-#ifdef BIRP_DEBUG_BOUNDS
             if (!bound_ok(pl - (C.nodes_ff[0] - 1), C.nodes_n, 4)) pl = C.nodes_ff[0];
             if (!bound_ok(ph - (C.nodes_ff[0] - 1), C.nodes_n, 4)) ph = C.nodes_ff[0];
-#endif
             const int il = ff_first_past(__ldg(pl), invk, Kk, cpk);
             const int ih = ff_first_past(__ldg(ph), invk, Kk, cpk);
+#else
+            const int il = ff_first_past(__ldg(C.nodes_ff[k]), invk, Kk, cpk);
+            const int ih = ff_first_past(__ldg(C.nodes_ff[k] + (A.n - 1)), invk, Kk, cpk);
+#endif
             if (il >= 0 && ih >= 0) {
               // moving up the ray enters at the first plane, moving down at the last
               sk = invk.hi > 0.f ? il : ih;
@@ -1080,11 +1090,13 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         } else {
           // within the bound: the oracle's predicate decides
           ++n_fp64;
-          long long ci = nd - C.nodes_ff[k];
 #ifdef BIRP_DEBUG_BOUNDS
+          long long ci = nd - C.nodes_ff[k];
           if (!bound_ok(ci, C.ax[k].n, 8)) ci = 0;
-#endif
           const double c = C.ax[k].c64[ci];
+#else
+          const double c = C.ax[k].c64[nd - C.nodes_ff[k]];
+#endif
           const float uc = u.hi + u.lo;
           i = exact_first_past_ray(sm.A[lx], sm.B[ly], k, R.pos[k], R.dt, c, inv[k].hi > 0.f,
                                    max((int)floorf(uc - E) - 1, 0), min((int)ceilf(uc + E) + 2, N));
@@ -1108,11 +1120,13 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           i = max((int)n0 + (dist > 0.f ? 1 : 0), 0);
         } else {
           ++n_fp64;
-          long long ci = nd - C.nodes_ff[k];
 #ifdef BIRP_DEBUG_BOUNDS
+          long long ci = nd - C.nodes_ff[k];
           if (!bound_ok(ci, C.ax[k].n, 8)) ci = 0;
-#endif
           const double c = C.ax[k].c64[ci];
+#else
+          const double c = C.ax[k].c64[nd - C.nodes_ff[k]];
+#endif
           const float uc = u.hi + u.lo;
           i = exact_first_past_ray(sm.A[lx], sm.B[ly], k, R.pos[k], R.dt, c, invk.hi > 0.f,
                                    max((int)floorf(uc - E) - 1, 0), min((int)ceilf(uc + E) + 2, N));
