@@ -67,14 +67,25 @@ extern "C" birp_status birp_batch_render_noalloc(const birp_request* reqs, int n
   if (n > kNoAllocMaxRequests)
     return fail(BIRP_ERR_INVALID, "%d requests exceed the no-allocation limit of %d per call", n, kNoAllocMaxRequests);
   if (n == 0) return ok();
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(BIRP_ERR_INVALID, "device %d out of range", dev);
+  // the library's device, as every other entry point: a call from a thread
+  // whose current device is another GPU is switched to it (the cubes' device
+  // descriptors live there)
+  if (birp_status s = check_init()) return s;
+  const int dev = g_ctx.device;
+  if (dev >= kMaxDevices) return fail(BIRP_ERR_INVALID, "device %d out of range", dev);
+  cudaStream_t st = pick_stream(stream);
+  // The request table is staged in one host array and copied from there: a
+  // captured copy would keep reading that array at every replay, which by
+  // then holds the latest call's requests, so a capturing stream is refused.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(st, &cap);
+  if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "cudaStreamIsCapturing: %s", cudaGetErrorString(e));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(BIRP_ERR_INVALID, "the stream is capturing: this call stages its requests in host memory that the "
+                                  "next call overwrites, so it cannot be recorded into a graph");
   unsigned char* scratch = nullptr;
   const int* grid = nullptr;
   if (birp_status s = setup_device(dev, &scratch, &grid)) return s;
-  cudaStream_t st = stream ? (cudaStream_t)stream : (g_ctx.device == dev ? g_ctx.stream : (cudaStream_t)0);
 
   std::lock_guard<std::mutex> lk(g_stage_mu);
   int* hdr = reinterpret_cast<int*>(g_stage);

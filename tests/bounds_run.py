@@ -2,7 +2,8 @@
 the bounds-checking library: renders every kernel class and edge case the
 walks have (both layouts, both interpolations, both march modes, rays from
 inside, outside and along the faces, negative values, thin cells, a far cube
-that tests every sample, CMEM, one mixed batch), checks each image against
+that tests every sample, CMEM, one mixed batch, the same mix through the
+no-allocation entry point), checks each image against
 the FP64 oracle, and exits 0 only if no table access was out of range."""
 import os
 import sys
@@ -111,6 +112,28 @@ def main():
     outs = b.render(items)
     n_img += len(outs)
     b.close()
+    # the same mix through the no-allocation entry point, whose one launch
+    # takes the general kernel (every class in one kernel), into device
+    # buffers; each image against the FP64 oracle
+    import ctypes as C
+    import torch
+    fn = B.lib().birp_batch_render_noalloc
+    fn.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    fn.restype = C.c_int
+    dev = [torch.full((c.ny * c.nx,), float("nan"), dtype=torch.float32, device="cuda:0") for _, c in items]
+    torch.cuda.synchronize()
+    ptrs = (C.c_void_p * len(dev))(*[d.data_ptr() for d in dev])
+    B.check(fn(B.Batch._reqs(items), len(items), ptrs, None))
+    torch.cuda.synchronize()
+    o_space = {id(gr): O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 1),
+               id(gc): O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 1), id(cm): O.Cmem64()}
+    o_nearest = O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 0)
+    for (sp, cam), d in zip(items, dev):
+        img = d.cpu().numpy().reshape(cam.ny, cam.nx)
+        ref = O.render64(o_space[id(sp)] if cam.trilinear else o_nearest, o_cam(cam), threads=THREADS)
+        mx, _, _ = rel_err(img, ref)
+        assert mx <= 1e-5 and np.array_equal(img == 0, ref == 0), (mx, tuple(cam.pos))
+        n_img += 1
     status = B.debug_bounds(reset=False)
     print(f"bounds-checked images: {n_img}; status {status:#x}")
     return 0 if status == 0 else 1
