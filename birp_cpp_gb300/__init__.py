@@ -31,7 +31,7 @@ class Camera(C.Structure):
     _fields_ = [("pos", C.c_double * 3), ("aim", C.c_double * 3), ("fov_w_deg", C.c_double),
                 ("fov_h_deg", C.c_double), ("nx", C.c_int), ("ny", C.c_int), ("n_samples", C.c_int),
                 ("ray_length", C.c_double), ("trilinear", C.c_int), ("march", C.c_int),
-                ("segments", C.c_int)]
+                ("segments", C.c_int), ("roll_deg", C.c_double)]
 
 
 class CmemParams(C.Structure):
@@ -126,7 +126,7 @@ def lib():
             "birp_time_render_device": ([P, P, P, P, I, I, P], I),
             "birp_cmem_margin_check": ([P, I, P, P], I),
             "birp_flush_l2": ([], I),
-            "birp_measure_peaks": ([P, P], I),
+            "birp_measure_peaks": ([P, P, P], I),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -154,7 +154,7 @@ def shutdown() -> None:
 
 
 def camera(pos, aim, fov_w, fov_h, nx, ny, n_samples=200, ray_length=44.0, trilinear=True, march=PREFIX,
-           segments=0) -> Camera:
+           segments=0, roll=0.0) -> Camera:
     c = Camera()
     for i in range(3):
         c.pos[i] = float(pos[i])
@@ -162,6 +162,7 @@ def camera(pos, aim, fov_w, fov_h, nx, ny, n_samples=200, ray_length=44.0, trili
     c.fov_w_deg, c.fov_h_deg, c.nx, c.ny = float(fov_w), float(fov_h), int(nx), int(ny)
     c.n_samples, c.ray_length = int(n_samples), float(ray_length)
     c.trilinear, c.march, c.segments = int(bool(trilinear)), int(march), int(segments)
+    c.roll_deg = float(roll)
     return c
 
 
@@ -294,11 +295,12 @@ def flush_l2() -> None:
     check(lib().birp_flush_l2())
 
 
-def measure_peaks() -> tuple[float, float]:
-    """(FP32 TFLOP/s, L2-resident read GB/s) measured on this GPU."""
-    f, r = C.c_double(), C.c_double()
-    check(lib().birp_measure_peaks(C.byref(f), C.byref(r)))
-    return f.value, r.value
+def measure_peaks() -> tuple[float, float, int]:
+    """(FP32 TFLOP/s, L2-resident read GB/s, buffer bytes of that read rate)
+    measured on this GPU."""
+    f, r, n = C.c_double(), C.c_double(), C.c_size_t()
+    check(lib().birp_measure_peaks(C.byref(f), C.byref(r), C.byref(n)))
+    return f.value, r.value, n.value
 
 
 class Batch:

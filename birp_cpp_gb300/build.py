@@ -19,6 +19,7 @@ LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libbirp_gb300.so")
 CLASSES_LIB = os.path.join(LIBDIR, "libbirp_classes.so")
 CPP = os.path.join(HERE, "cpp")
+ABI_INCLUDE = os.path.normpath(os.path.join(HERE, "..", "include"))  # include/birp_gb300.h, the C ABI
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["render.cu", "capi.cu", "cube.cu", "batch.cu", "server.cu", "noalloc.cu", "cmem_host.cpp", "tune.cpp"]
@@ -99,7 +100,7 @@ def build_cli() -> str:
                                  for h in os.listdir(os.path.join(CPP, "include", "birp"))]
     if os.path.exists(CLI) and all(os.path.getmtime(CLI) >= os.path.getmtime(d) for d in deps):
         return CLI
-    cmd = ["g++", "-O2", "-std=c++17", "-Wall", src, "-I", os.path.join(CPP, "include"), "-L", LIBDIR,
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", src, "-I", os.path.join(CPP, "include"), "-I", ABI_INCLUDE, "-L", LIBDIR,
            "-lbirp_classes", "-lbirp_gb300", "-lpthread", "-Wl,-rpath,$ORIGIN", "-o", CLI]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -110,11 +111,12 @@ def build_cli() -> str:
 def build_classes() -> str:
     """The reference-API C++ classes (cpp/) over the C ABI: libbirp_classes.so."""
     srcs = [os.path.join(CPP, "src", f) for f in ("classes.cpp", "helper.cpp")]
-    deps = srcs + [LIB] + [os.path.join(CPP, "include", "birp", h)
+    deps = srcs + [LIB, os.path.join(ABI_INCLUDE, "birp_gb300.h")] + [os.path.join(CPP, "include", "birp", h)
                            for h in os.listdir(os.path.join(CPP, "include", "birp"))]
     if os.path.exists(CLASSES_LIB) and all(os.path.getmtime(CLASSES_LIB) >= os.path.getmtime(d) for d in deps):
         return CLASSES_LIB
     cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-Wall", *srcs, "-I", os.path.join(CPP, "include"),
+           "-I", ABI_INCLUDE,
            "-L", LIBDIR, "-lbirp_gb300", "-Wl,-rpath,$ORIGIN", "-o", CLASSES_LIB]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -30,6 +30,9 @@ class Camera {
   void SetStep(double step, double ray_length = 44.0);
   void SetMarchMode(int mode);
   void SetSegments(int lanes);
+  // Extension: roll about the view axis in degrees, added to the Sun-fixed
+  // roll that Orient computes (0, the default, is the reference's pose).
+  void SetRoll(double degrees);
   int Width() const { return image_dimension_x; }
   int Height() const { return image_dimension_y; }
 
@@ -48,6 +51,7 @@ class Camera {
   double ray_length = 44.0;
   int march = 0;
   int segments = 0;
+  double roll_deg = 0.0;
 };
 
 // Renders several cameras (any mix of DataCubes and CMEM) in one batched GPU

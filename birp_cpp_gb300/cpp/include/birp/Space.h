@@ -4,7 +4,7 @@
 // fused GB300 kernels instead of calling GetSample per sample.
 #pragma once
 
-#include "../../../../include/birp_gb300.h"  // the C ABI the classes call
+#include "birp_gb300.h"  // the C ABI the classes call (the include/ directory on the include path)
 
 class Space {
  public:

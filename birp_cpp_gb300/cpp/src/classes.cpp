@@ -375,6 +375,8 @@ void Camera::SetMarchMode(int mode) { march = mode; }
 
 void Camera::SetSegments(int lanes) { segments = lanes; }
 
+void Camera::SetRoll(double degrees) { roll_deg = degrees; }
+
 birp_camera Camera::Describe() const {
   birp_camera c;
   std::memset(&c, 0, sizeof c);
@@ -393,6 +395,7 @@ birp_camera Camera::Describe() const {
   c.trilinear = dataCube->Trilinear() ? 1 : 0;
   c.march = march;
   c.segments = segments;
+  c.roll_deg = roll_deg;
   return c;
 }
 

@@ -112,7 +112,9 @@ double sun_roll_deg(const double* pos, const double* aim) {
 birp_status camera_frame(const birp_camera& c, Frame& f) {
   const double to_rad = M_PI / 180.0;
   f.angle_sun = sun_roll_deg(c.pos, c.aim);
-  double asc = 180.0 - f.angle_sun;
+  // the caller's roll offset adds to the Sun-fixed roll (0: exactly the
+  // reference's angle)
+  double asc = 180.0 - (f.angle_sun + c.roll_deg);
   double xd = c.aim[0] - c.pos[0];
   double theta = 2 * M_PI - std::atan2(xd, c.pos[1]);
   double hyp = std::sqrt(xd * xd + c.pos[1] * c.pos[1]);
@@ -668,16 +670,18 @@ birp_status birp_flush_l2(void) {
   return ok();
 }
 
-birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs) {
+birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs, size_t* l2_buffer_bytes) {
   if (birp_status s = check_init()) return s;
   std::lock_guard<std::mutex> lk(g_ctx.mu);
   cudaStream_t st = g_ctx.stream;
   float* sink = nullptr;
   float4* buf = nullptr;
-  // L2 read rate: the largest over L2-resident buffers of 8, 16 and 32 MB
+  // L2 read rate: the largest over L2-resident buffers of 16, 32 and 64 MB
   // (where a buffer's lines sit in the two dies' L2 halves varies with the
-  // allocation), each launch reading about 2 GB, best of 3 launches per size
-  const size_t max_bytes = (size_t)32 << 20;
+  // allocation), read with loads that bypass L1 (a grid-stride pass gives
+  // each SM the same slice in every repetition, which L1 would otherwise
+  // serve), each launch reading about 2 GB, best of 3 launches per size
+  const size_t max_bytes = (size_t)64 << 20;
   CK(cudaMalloc(&sink, sizeof(float)));
   CK(cudaMalloc(&buf, max_bytes));
   CK(cudaMemsetAsync(buf, 0, max_bytes, st));
@@ -687,6 +691,7 @@ birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs) {
   const int blocks = g_ctx.sms * 8, iters = 20000;
   float best_f = 1e30f;
   double best_gbs = 0.0;
+  size_t best_bytes = 0;
   for (int rep = 0; rep < 3; ++rep) {
     float ms;
     CK(cudaEventRecord(e0, st));
@@ -696,7 +701,7 @@ birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs) {
     CK(cudaEventElapsedTime(&ms, e0, e1));
     best_f = std::min(best_f, ms);
   }
-  for (size_t bytes : {(size_t)8 << 20, (size_t)16 << 20, max_bytes}) {
+  for (size_t bytes : {(size_t)16 << 20, (size_t)32 << 20, max_bytes}) {
     const int reps = (int)(((size_t)2 << 30) / bytes);
     CK(launch_peak_read(buf, bytes / 16, 1, sink, g_ctx.sms * 4, st));  // bring the buffer into L2
     for (int rep = 0; rep < 3; ++rep) {
@@ -706,7 +711,11 @@ birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs) {
       CK(cudaEventRecord(e1, st));
       CK(cudaEventSynchronize(e1));
       CK(cudaEventElapsedTime(&ms, e0, e1));
-      best_gbs = std::max(best_gbs, (double)bytes * reps / (ms * 1e-3) / 1e9);
+      const double gbs = (double)bytes * reps / (ms * 1e-3) / 1e9;
+      if (gbs > best_gbs) {
+        best_gbs = gbs;
+        best_bytes = bytes;
+      }
     }
   }
   cudaEventDestroy(e0);
@@ -715,6 +724,7 @@ birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs) {
   cudaFree(buf);
   if (fp32_tflops) *fp32_tflops = 2.0 * 8 * iters * (double)blocks * 256 / (best_f * 1e-3) / 1e12;
   if (l2_read_gbs) *l2_read_gbs = best_gbs;
+  if (l2_buffer_bytes) *l2_buffer_bytes = best_bytes;
   return ok();
 }
 

@@ -142,6 +142,34 @@ def config2_requests(n: int = 512, seed: int = 2):
             for i in range(n)]
 
 
+def config2_rolls(n: int = 512, seed: int = 2) -> np.ndarray:
+    """Camera roll of each config-2 request in degrees, uniform in [-10, 10]
+    (drawn from its own stream, so the poses, sizes and steps of
+    config2_requests are unchanged)."""
+    return np.random.default_rng(seed + 7919).uniform(-10.0, 10.0, n)
+
+
+def serving_bases(nx: int, ny: int, nz: int, r0s=(7.5, 9.0, 10.5, 12.0)):
+    """Axes and noise-free FP32 base fields of the serving pool's cubes, one
+    per standoff r0 group."""
+    xs, ys, zs = stretched_axis(-40, 30, nx), stretched_axis(-40, 40, ny), stretched_axis(-40, 40, nz)
+    bases = [sheath_field(xs, ys, zs, np.random.default_rng(40 + g), r0=r0, noise=0.0).astype(np.float32)
+             for g, r0 in enumerate(r0s)]
+    return xs, ys, zs, bases
+
+
+def serving_cube(i: int, bases) -> np.ndarray:
+    """FP32 values of serving cube i: its group's base field times
+    (1 + 0.3 N), N uniform in [-1, 1] per node from the cube's own seed,
+    computed in FP32 in place (the same values on every call)."""
+    base = bases[i % len(bases)]
+    v = np.random.default_rng(1000 + i).random(base.shape, dtype=np.float32)
+    v *= np.float32(0.6)
+    v += np.float32(0.7)
+    v *= base
+    return v
+
+
 def cube_stretched(nx: int, ny: int, nz: int, r0: float, seed: int, noise: float = 0.3):
     """A cube with the config-1 axis rule on x in [-40, 30], y, z in [-40, 40]
     and its own magnetopause standoff r0 (bow shock at 1.3 r0)."""

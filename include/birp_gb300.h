@@ -120,7 +120,10 @@ typedef enum { BIRP_MARCH_PREFIX = 0, BIRP_MARCH_CLIP = 1 } birp_march;
  * n_samples. PREFIX stops a ray at its first sample below zero: out of the
  * box, or a negative cube value (the reference, src/Camera.cpp:205-209);
  * CLIP skips such samples up to the first good one and stops at the next.
- * segments: lanes per ray (1, 2, 4, 8), 0 = tuned choice. */
+ * segments: lanes per ray (1, 2, 4, 8), 0 = tuned choice. roll_deg: a roll
+ * about the view axis in degrees, added to the Sun-fixed roll angle of
+ * Camera::Orient (src/Camera.cpp:309-417); 0 (the default) is the
+ * reference's pose exactly (an extension: the reference has no roll input). */
 typedef struct {
   double pos[3];
   double aim[3];
@@ -131,6 +134,7 @@ typedef struct {
   int trilinear;
   int march;
   int segments;
+  double roll_deg;
 } birp_camera;
 
 /* Fills the reference's CLI defaults (src/main.cpp:37-63): pos
@@ -197,11 +201,14 @@ birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, fl
  * one DEVICE output buffer of ny*nx floats per request; the only other device
  * memory used is a 64 KB array inside this library (held on every GPU that
  * loads it), set up by the first call on each device (make that first call
- * before any stream capture). Asynchronous on `stream` (NULL: the library's
- * stream if initialised on this device, else the default stream). Every call
- * shares that array, so calls whose work overlaps on the GPU race: order them
- * on one stream. More than 256 requests is BIRP_ERR_INVALID. No counterpart in
- * the reference. */
+ * before any stream capture). Runs on the library's device (birp_init), as
+ * the other entry points, from any host thread. Asynchronous on `stream`
+ * (NULL: the library's stream). A stream that is capturing is refused with
+ * BIRP_ERR_INVALID: the request table is copied from a host array that the
+ * next call overwrites. Every call shares the device array, so calls whose
+ * work overlaps on the GPU race: order them on one stream. More than 256
+ * requests, or a NULL output, is BIRP_ERR_INVALID; n = 0 does nothing. No
+ * counterpart in the reference. */
 birp_status birp_batch_render_noalloc(const birp_request* reqs, int n, float* const* outs_device, void* stream);
 
 /* Device time of the batch's last launch in ms (CUDA events around the
@@ -293,8 +300,11 @@ birp_status birp_time_render_device(const birp_cube* cube, const birp_cmem* cmem
 birp_status birp_flush_l2(void);
 
 /* Roofline denominators measured on this GPU: FP32 FMA throughput (TFLOP/s,
- * FMA = 2 flops) and the read bandwidth of an L2-resident buffer (GB/s). */
-birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs);
+ * FMA = 2 flops) and the read bandwidth of an L2-resident buffer (GB/s; loads
+ * that bypass L1, the best over 16, 32 and 64 MB buffers, whose size is
+ * returned in l2_buffer_bytes). Any output may be NULL. No counterpart in the
+ * reference. */
+birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs, size_t* l2_buffer_bytes);
 
 /* Largest FP32 error of the CMEM boundary radii against FP64 over n
  * directions, relative to (|r| + 5 Re), where the radius is under 100 Re (a

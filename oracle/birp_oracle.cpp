@@ -118,6 +118,7 @@ typedef struct {
   int n_samples;        // N
   double ray_length;    // L; dt = L / N
   int mode;             // 0 prefix (reference), 1 clip
+  double roll;          // degrees added to the Sun-fixed roll (extension; 0 = reference)
 } o64_camera;
 
 // space kinds for the render entry points
@@ -563,9 +564,9 @@ double det3d(const double v[3][3]) {
 }
 
 // R^-1 (cofactor inverse, as the reference) in double. rinv[r][c].
-bool pose64(const double* position, const double* aim, double rinv[3][3]) {
+bool pose64(const double* position, const double* aim, double roll, double rinv[3][3]) {
   const double to_rad = M_PI / 180.0;
-  double asc = 180.0 - orient64(position, aim);
+  double asc = 180.0 - (orient64(position, aim) + roll);
   double x_diff = aim[0] - position[0];
   double theta = 2 * M_PI - std::atan2(x_diff, position[1]);
   double hyp = std::sqrt(x_diff * x_diff + position[1] * position[1]);
@@ -614,7 +615,7 @@ struct Frame64 {
 };
 
 bool frame64(const o64_camera* c, Frame64* f) {
-  if (!pose64(c->pos, c->aim, f->rinv)) return false;
+  if (!pose64(c->pos, c->aim, c->roll, f->rinv)) return false;
   const double to_rad = M_PI / 180.0;
   f->aspect = (double)c->nx / (double)c->ny;
   f->tfx = std::tan(to_rad * (c->fov_w / 2.0));

@@ -65,7 +65,7 @@ class O32Camera(C.Structure):
 class O64Camera(C.Structure):
     _fields_ = [("pos", C.c_double * 3), ("aim", C.c_double * 3), ("fov_w", C.c_double),
                 ("fov_h", C.c_double), ("nx", C.c_int), ("ny", C.c_int), ("n_samples", C.c_int),
-                ("ray_length", C.c_double), ("mode", C.c_int)]
+                ("ray_length", C.c_double), ("mode", C.c_int), ("roll", C.c_double)]
 
 
 def build(quiet: bool = True) -> str:
@@ -224,13 +224,14 @@ def camera32(pos, aim, fov_w, fov_h, nx, ny, n_samples=200, ray_max=44, mode=PRE
     return c
 
 
-def camera64(pos, aim, fov_w, fov_h, nx, ny, n_samples=200, ray_length=44.0, mode=PREFIX) -> O64Camera:
+def camera64(pos, aim, fov_w, fov_h, nx, ny, n_samples=200, ray_length=44.0, mode=PREFIX,
+             roll=0.0) -> O64Camera:
     c = O64Camera()
     for i in range(3):
         c.pos[i] = pos[i]
         c.aim[i] = aim[i]
     c.fov_w, c.fov_h, c.nx, c.ny = fov_w, fov_h, nx, ny
-    c.n_samples, c.ray_length, c.mode = n_samples, ray_length, mode
+    c.n_samples, c.ray_length, c.mode, c.roll = n_samples, ray_length, mode, roll
     return c
 
 

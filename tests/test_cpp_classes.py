@@ -14,7 +14,8 @@ def _compile(src, out):
     from birp_cpp_gb300 import build
     build.build()
     cmd = ["g++", "-O2", "-std=c++17", "-pthread", os.path.join(ROOT, "tests", "cpp", src), "-I",
-           os.path.join(ROOT, "birp_cpp_gb300", "cpp", "include"), "-L", LIBDIR, "-lbirp_classes", "-lbirp_gb300",
+           os.path.join(ROOT, "birp_cpp_gb300", "cpp", "include"), "-I", os.path.join(ROOT, "include"), "-L", LIBDIR,
+           "-lbirp_classes", "-lbirp_gb300",
            f"-Wl,-rpath,{LIBDIR}", "-o", out]
     subprocess.run(cmd, check=True)
 

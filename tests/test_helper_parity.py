@@ -36,7 +36,8 @@ def ours(tmp_path_factory):
     build.build()
     out = str(tmp_path_factory.mktemp("helper") / "libhelper_ours.so")
     subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", os.path.join(ROOT, "oracle", "helper_shim.cpp"),
-                    "-I", os.path.join(ROOT, "birp_cpp_gb300", "cpp", "include", "birp"), "-L", LIBDIR,
+                    "-I", os.path.join(ROOT, "birp_cpp_gb300", "cpp", "include", "birp"),
+                    "-I", os.path.join(ROOT, "include"), "-L", LIBDIR,
                     "-lbirp_classes", "-lbirp_gb300", f"-Wl,-rpath,{LIBDIR}", "-o", out], check=True)
     return _bind(C.CDLL(out))
 
