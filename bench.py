@@ -1,10 +1,11 @@
 """Benchmark of the GB300 BIRP render path.
 
-Workload (default): 512 renders of a 256^3 stretched-axis FP32 cube (x in
-[-40, 30], y, z in [-40, 40] Re, trilinear, PREFIX march), poses on the
-SMILE-like orbit aimed at (9, 0, 0), image sizes from {144x84, 288x168,
-576x336, 1024x600} and steps from {0.025, 0.05, 0.1} Re, seeded. One step =
-one pass over all 512 requests.
+Headline workload (config 2 on config 1's cube): 512 renders of a 256^3
+stretched-axis FP32 cube (x in [-40, 30], y, z in [-40, 40] Re, trilinear,
+PREFIX march), poses on the SMILE-like orbit aimed at (9, 0, 0) with a roll
+uniform in [-10, 10] deg, image sizes from {144x84, 288x168, 576x336,
+1024x600} and steps from {0.025, 0.05, 0.1} Re, seeded. One step = one pass
+over all 512 requests.
 
   value      images/s of the batched path (one persistent-kernel launch from a
              CUDA graph), device time, inputs resident, L2 flushed between steps
@@ -13,6 +14,9 @@ one pass over all 512 requests.
   plain      images/s of the one-render-per-call path (birp_render, host output)
   serving    p50/p99 latency of the continuous-batching server at 70% of the
              saturated rate (Poisson arrivals)
+  parity     max and RMS relative error of EVERY timed image against the FP64
+             oracle on a random pixel sample of each image, plus one whole
+             image per size class
   roofline   the batched kernel against the slower of its FP32 work and its
              gathered bytes at the L2 read rate, both peaks measured in-run;
              roofline_issue: its warp instructions (per cell segment, from the
@@ -21,9 +25,19 @@ one pass over all 512 requests.
   cpu_baseline  the reference's FP32 render arithmetic (oracle port) on all
              host cores over a bounded random pixel sample of the same
              workload, and on one core
+  c3         config 3: 48 uneven stretched cubes x 16 cameras + 8 CMEM
+             requests in one launch vs plain renders, with per-image parity
+  c4         config 4: the serving sweep over 256 cubes of 512x384x384 (77 GB
+             of host data) under a 60 GB device budget, Poisson arrivals at
+             rising rates until the served rate falls behind the offered one,
+             then p50/p99 at 70% of that saturated rate, with parity of
+             served images
 
-`--impl reference` times only that CPU implementation (bounded samples).
-Multi-GPU (torchrun): replicas, one per rank, barrier + max over ranks.
+`--impl reference` times only the CPU implementation (bounded samples).
+`--workload c3|c4` runs one of the extra blocks alone; `--profile-case
+trilinear|nearest|compact|cmem` runs a small fixed batch to profile one
+kernel class. Multi-GPU (torchrun): replicas, one per rank, barrier + max
+over ranks (the c3/c4 blocks run at N = 1 only).
 """
 from __future__ import annotations
 
@@ -136,7 +150,90 @@ class ClockSampler:
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ---------------------------------------------------------------- workload
+# ---------------------------------------------------------------- oracle checks
+
+def oracle():
+    """The CPU oracle (test infrastructure): here only the checker of the
+    timed images and the CPU baseline."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as O
+    O.build()
+    return O
+
+
+def o_camera(O, cam):
+    """The FP64 oracle's camera for a C-ABI camera (roll included)."""
+    return O.camera64(tuple(cam.pos), tuple(cam.aim), cam.fov_w_deg, cam.fov_h_deg, cam.nx, cam.ny, cam.n_samples,
+                      cam.ray_length, cam.march, cam.roll_deg)
+
+
+def image_error(O, space, cam, img, n_px: int, seed: int):
+    """Max and RMS relative error of one image against the FP64 oracle on
+    n_px random pixels (all pixels if the image has fewer), over the pixels
+    above 1e-3 of the sample's largest reference value (the image maximum is
+    at least that large, so the threshold is no looser than the image's)."""
+    rng = np.random.default_rng(seed)
+    npx = cam.nx * cam.ny
+    flat = np.arange(npx) if npx <= n_px else rng.choice(npx, n_px, replace=False)
+    pi, pj = flat % cam.nx, flat // cam.nx
+    ref = O.render64_pixels(space, o_camera(O, cam), pi, pj, threads=1)
+    got = np.asarray(img).reshape(cam.ny, cam.nx)[pj, pi].astype(np.float64)
+    peak = np.abs(ref).max() if len(ref) else 0.0
+    m = np.abs(ref) > 1e-3 * peak if peak > 0 else np.zeros(len(ref), bool)
+    if not m.any():
+        # an all-zero view: every pixel must be exactly zero
+        return (0.0 if np.all(got == ref) else float("inf")), 0.0, 0
+    e = np.abs(got[m] - ref[m]) / np.abs(ref[m])
+    return float(e.max()), float(np.sqrt(np.mean(e * e))), int(m.sum())
+
+
+def parity_report(O, jobs, n_px: int, tol: float = 1e-5, label=None):
+    """jobs: (oracle space, camera, image) per image; every image is checked
+    on its own pixel sample, on all host cores (one oracle call per image)."""
+    import concurrent.futures as cf
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        res = list(ex.map(lambda a: image_error(O, a[1][0], a[1][1], a[1][2], n_px, 1000 + a[0]), enumerate(jobs)))
+    mx = np.array([r[0] for r in res])
+    rms = np.array([r[1] for r in res])
+    cnt = np.array([r[2] for r in res])
+    w = int(np.argmax(mx))
+    wc = jobs[w][1]
+    out = {"images": len(jobs), "pixels_per_image": n_px, "pixels_checked": int(cnt.sum()),
+           "max_rel_err": float(mx.max()), "rms_rel_err": float(np.sqrt(np.sum(rms * rms * cnt) / max(cnt.sum(), 1))),
+           "per_image_max_quantiles": {q: float(np.quantile(mx, p)) for q, p in
+                                       (("p50", .5), ("p90", .9), ("p99", .99), ("max", 1.0))},
+           "worst_image": {"index": w, "size": f"{wc.nx}x{wc.ny}", "n_samples": int(wc.n_samples),
+                           "max_rel_err": float(mx[w]), "rms_rel_err": float(rms[w])},
+           "images_within_tolerance": int(np.sum(mx <= tol)), "tolerance": tol,
+           "per_image": [[float(f"{a:.3g}"), float(f"{b:.3g}")] for a, b in zip(mx, rms)],
+           "check_s": time.perf_counter() - t0}
+    if label:
+        out["what"] = label
+    return out
+
+
+def full_image_checks(O, space, items, imgs):
+    """One whole image per size class against the FP64 oracle."""
+    seen, out = set(), []
+    threads = os.cpu_count() or 4
+    for (cam, img) in zip(items, imgs):
+        key = (cam.nx, cam.ny)
+        if key in seen:
+            continue
+        seen.add(key)
+        t0 = time.perf_counter()
+        ref = O.render64(space, o_camera(O, cam), threads=threads)
+        got = np.asarray(img, np.float64).reshape(cam.ny, cam.nx)
+        m = ref > 1e-3 * max(ref.max(), 1e-300)
+        e = np.abs(got[m] - ref[m]) / ref[m] if m.any() else np.zeros(1)
+        out.append({"size": f"{cam.nx}x{cam.ny}", "n_samples": int(cam.n_samples), "pixels": int(m.sum()),
+                    "max_rel_err": float(e.max()), "rms_rel_err": float(np.sqrt(np.mean(e * e))),
+                    "oracle_s": time.perf_counter() - t0})
+    return out
+
+
+# ---------------------------------------------------------------- workloads
 
 def make_workload(B, n_req: int, seed_cube: int = 1, seed_req: int = 2):
     from birp_cpp_gb300 import synth
@@ -144,8 +241,10 @@ def make_workload(B, n_req: int, seed_cube: int = 1, seed_req: int = 2):
     v32 = v64.astype(np.float32)
     cube = B.Cube(xs, ys, zs, v32)
     reqs = synth.config2_requests(n_req, seed=seed_req)
+    rolls = synth.config2_rolls(n_req, seed=seed_req)
     cams = [B.camera(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(step),
-                     ray_length=synth.RAY_LENGTH, trilinear=True) for pos, aim, nx, ny, step in reqs]
+                     ray_length=synth.RAY_LENGTH, trilinear=True, roll=float(r))
+            for (pos, aim, nx, ny, step), r in zip(reqs, rolls)]
     return dict(cube=cube, cams=cams, reqs=reqs, host=(xs, ys, zs, v32))
 
 
@@ -156,34 +255,33 @@ def _gen_cube(spec):
     return xs, ys, zs, v.astype(np.float32)
 
 
-def make_workload_c3(B, host_cubes, specs):
-    """Config 3: 48 uneven stretched cubes (16 cameras each) + 8 CMEM requests."""
-    from birp_cpp_gb300 import synth
-    cubes = [B.Cube(*hc) for hc in host_cubes]
-    cmem = B.Cmem()
-    items = []
-    for src, pos, aim, nx, ny, step in specs:
-        cam = B.camera(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(step),
-                       ray_length=synth.RAY_LENGTH, trilinear=True)
-        items.append((cubes[src] if src >= 0 else cmem, cam))
-    return cubes, cmem, items
-
-
-def run_c3(args, B):
-    """One-launch multi-cube batch (config 3) vs plain renders of the same requests."""
+def gen_c3_host():
+    """Config 3's 48 cubes, generated in a spawned process pool (safe before
+    or after the first GPU call)."""
     import concurrent.futures as cf
     import multiprocessing as mp
     from birp_cpp_gb300 import synth
     cube_specs, specs = synth.config3_specs()
     with cf.ProcessPoolExecutor(max_workers=os.cpu_count() or 4, mp_context=mp.get_context("spawn")) as ex:
         host = list(ex.map(_gen_cube, cube_specs))
-    from birp_cpp_gb300 import build
-    build.build()
-    B.init(0)
-    cubes, cmem, items = make_workload_c3(B, host, specs)
+    return host, specs
+
+
+def run_c3(args, B, O, host, specs):
+    """Config 3: 48 uneven stretched cubes (16 cameras each) + 8 CMEM requests
+    in one launch, against one plain call per request; every image checked
+    against the FP64 oracle on a pixel sample."""
+    from birp_cpp_gb300 import synth
+    cubes = [B.Cube(*hc) for hc in host]
+    cmem = B.Cmem()
+    items = []
+    for src, pos, aim, nx, ny, step in specs:
+        cam = B.camera(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(step),
+                       ray_length=synth.RAY_LENGTH, trilinear=True)
+        items.append((cubes[src] if src >= 0 else cmem, cam))
     total_px = sum(c.nx * c.ny for _, c in items)
     batch = B.Batch(len(items), total_px)
-    for _ in range(max(args.warmup, 2)):
+    for _ in range(max(args.warmup, 3)):
         batch.render(items)
     km = []
     for _ in range(args.steps):
@@ -192,101 +290,247 @@ def run_c3(args, B):
         batch.wait()
         km.append(batch.last_ms()[0])
     ms = float(np.mean(km))
+    imgs = batch.render(items)
+    # plain: one birp_render per request, host outputs
     outs = [np.empty((c.ny, c.nx), np.float32) for _, c in items]
-    t0 = time.perf_counter()
-    for (sp, c), o in zip(items, outs):
+    for (sp, c), o in zip(items[:8], outs[:8]):
         B.render(sp, c, out=o)
-    plain_s = time.perf_counter() - t0
+    pt = []
+    for _ in range(2):
+        B.flush_l2()
+        t0 = time.perf_counter()
+        for (sp, c), o in zip(items, outs):
+            B.render(sp, c, out=o)
+        pt.append(time.perf_counter() - t0)
+    plain_s = min(pt)
     dev_bytes = sum(c.info().device_bytes for c in cubes)
-    print(json.dumps({"workload": "config 3: 48 uneven stretched cubes x 16 cameras + 8 CMEM, one launch",
-                      "requests": len(items), "images_s": len(items) / (ms / 1000), "ms_per_launch": ms,
-                      "plain_images_s": len(items) / plain_s, "batched_vs_plain": (len(items) / (ms / 1000)) /
-                      (len(items) / plain_s), "cube_device_bytes": dev_bytes}))
+    batch.close()
+    # parity: cube by cube (one FP64 oracle copy at a time), then CMEM
+    jobs_err = [None] * len(items)
+    t0 = time.perf_counter()
+    for ci, (xs, ys, zs, v32) in enumerate(host):
+        idx = [k for k, (src, *_r) in enumerate(specs) if src == ci]
+        if not idx:
+            continue
+        oc = O.Cube64(xs, ys, zs, v32.astype(np.float64), 1)
+        rep = parity_report(O, [(oc, items[k][1], imgs[k]) for k in idx], args.parity_px)
+        for k, (a, b) in zip(idx, rep["per_image"]):
+            jobs_err[k] = (a, b)
+        del oc
+    idx = [k for k, (src, *_r) in enumerate(specs) if src < 0]
+    rep_cmem = parity_report(O, [(O.Cmem64(), items[k][1], imgs[k]) for k in idx], args.parity_px)
+    for k, (a, b) in zip(idx, rep_cmem["per_image"]):
+        jobs_err[k] = (a, b)
+    mx = np.array([e[0] for e in jobs_err])
+    w = int(np.argmax(mx))
+    parity = {"images": len(items), "pixels_per_image": args.parity_px, "max_rel_err": float(mx.max()),
+              "per_image_max_quantiles": {q: float(np.quantile(mx, p)) for q, p in
+                                          (("p50", .5), ("p90", .9), ("p99", .99), ("max", 1.0))},
+              "worst_image": {"index": w, "source": "cmem" if specs[w][0] < 0 else f"cube {specs[w][0]}",
+                              "size": f"{items[w][1].nx}x{items[w][1].ny}", "max_rel_err": float(mx[w])},
+              "cmem_max_rel_err": rep_cmem["max_rel_err"],
+              "images_within_tolerance": int(np.sum(mx <= 1e-5)), "tolerance": 1e-5,
+              "per_image": [list(e) for e in jobs_err], "check_s": time.perf_counter() - t0}
+    for c in cubes:
+        c.close()
+    cmem.close()
+    n = len(items)
+    return {"workload": "config 3: 48 uneven stretched cubes (dims multiples of 16 in [96, 320], r0 in U[7, 12]) "
+                        "x 16 orbit cameras + 8 CMEM requests, one launch",
+            "requests": n, "images_s": n / (ms / 1000), "ms_per_launch": ms, "plain_images_s": n / plain_s,
+            "batched_vs_plain": (n / (ms / 1000)) / (n / plain_s), "cube_device_bytes": dev_bytes,
+            "total_pixels": total_px, "parity": parity}
 
 
-def run_c4(args, B):
-    """Serving sweep (config 4): Poisson arrivals at each rate for a fixed time;
-    requests pick a cube by Zipf(1.1) popularity over a pool of cubes held in
-    host (pinned) memory, rendered through the server under a GPU byte budget
-    with LRU eviction; poses, sizes and steps from the orbit sampler.
-    Reports images/s and p50/p99 latency per rate beside the plain per-call
-    render's latency."""
-    from birp_cpp_gb300 import build, synth
+def run_c4(args, B, O):
+    """Config 4, the serving sweep: Poisson arrivals at each offered rate for a
+    fixed time; each request picks a cube by Zipf(1.1) popularity over a pool
+    of cubes held in host (pinned) memory, rendered through the server under a
+    GPU byte budget with LRU eviction; poses, sizes and steps from the orbit
+    sampler. The sweep rises until the served rate falls behind the offered
+    one (saturation); then one run at 70% of the saturated rate gives the
+    p50/p99 the target is stated at. Served images of a few cubes (popular
+    and rarely used, so some were evicted and re-uploaded) are checked
+    against the FP64 oracle."""
+    import concurrent.futures as cf
+    from birp_cpp_gb300 import synth
     nx, ny, nz = (int(v) for v in args.c4_dims.split("x"))
-    rng = np.random.default_rng(4)
-    # a few base fields (standoff r0 groups) and per-cube sheath noise
-    xs, ys, zs = synth.stretched_axis(-40, 30, nx), synth.stretched_axis(-40, 40, ny), synth.stretched_axis(-40, 40, nz)
-    r0_groups = [7.5, 9.0, 10.5, 12.0]
-    bases = [synth.sheath_field(xs, ys, zs, np.random.default_rng(40 + g), r0=r0, noise=0.0).astype(np.float32)
-             for g, r0 in enumerate(r0_groups)]
-    build.build()
-    B.init(0)
+    n_cubes = args.c4_cubes
+    t_setup = time.perf_counter()
+    xs, ys, zs, bases = synth.serving_bases(nx, ny, nz)
     layout = B.CUBE_COMPACT if args.c4_layout == "compact" else B.CUBE_RECORDS
     srv = B.Server(B.server_config(cube_budget_bytes=int(args.c4_budget_gb * (1 << 30)), slots=3,
                                    max_batch_requests=64, max_batch_pixels=16 << 20, max_wait_ms=1.0,
-                                   max_queue=1 << 16, cube_layout=layout))
-    ids = []
-    for i in range(args.c4_cubes):
-        # base * (1 + 0.3 U(-1, 1)), in FP32 and in place (256 cubes of 75 M
-        # nodes are generated in minutes)
-        v = rng.random(bases[0].shape, dtype=np.float32)
-        v *= np.float32(0.6)
-        v += np.float32(0.7)
-        v *= bases[i % len(bases)]
-        ids.append(srv.add_cube(xs, ys, zs, v))
-        del v
-    zipf_w = 1.0 / np.arange(1, args.c4_cubes + 1) ** 1.1
+                                   max_queue=1 << 17, cube_layout=layout))
+
+    def add(i):
+        return srv.add_cube(xs, ys, zs, synth.serving_cube(i, bases))
+
+    with cf.ThreadPoolExecutor(max_workers=8) as ex:
+        ids = list(ex.map(add, range(n_cubes)))
+    setup_s = time.perf_counter() - t_setup
+    zipf_w = 1.0 / np.arange(1, n_cubes + 1) ** 1.1
     zipf_w /= zipf_w.sum()
+    rng = np.random.default_rng(4)
     reqs = synth.config2_requests(8192, seed=44)
-    cams = [B.camera(p, a, synth.FOV_W, synth.FOV_H, w, h, n_samples=synth.n_samples(st)) for p, a, w, h, st in reqs]
+    rolls = synth.config2_rolls(8192, seed=44)
+    cams = [B.camera(p, a, synth.FOV_W, synth.FOV_H, w, h, n_samples=synth.n_samples(st), roll=float(r))
+            for (p, a, w, h, st), r in zip(reqs, rolls)]
     max_px = max(c.nx * c.ny for c in cams)
     # written once here: a client reuses its result buffers, and the first
-    # touch of fresh pages (OS zero-fill, ~100 ms process-wide stalls at
-    # 2.5 GB) is allocation cost, not serving latency
+    # touch of fresh pages is allocation cost, not serving latency
     bufs = [np.full(max_px, 0.0, np.float32) for _ in range(1024)]
-    results = []
-    for rate in (float(r) for r in args.c4_rates.split(",")):
-        t0 = time.perf_counter()
-        nxt, k, tickets = t0, 0, []
+    # warm start: the most popular cubes resident (requests in reverse
+    # popularity order, so the LRU keeps the popular ones)
+    t0 = time.perf_counter()
+    small = [c for c in cams if c.nx == 144][:1]
+    tk = [srv.submit(ids[r], small[0], bufs[r % len(bufs)]) for r in range(n_cubes - 1, -1, -1)]
+    for t in tk:
+        srv.wait(t, 600000)
+    warm_s = time.perf_counter() - t0
+    st_warm = srv.stats()
+    # parity probes: the first requests to these popularity ranks in each
+    # phase get their own buffers
+    probe_ranks = sorted({0, 1, 4, min(30, n_cubes - 1), min(120, n_cubes - 1), n_cubes - 1})
+    probes = []
+
+    def phase(rate, seconds, max_probes_per_rank=1):
+        picks = rng.choice(n_cubes, size=int(rate * seconds * 1.3) + 64, p=zipf_w)
+        gaps = rng.exponential(1.0 / rate, size=len(picks))
+        per_rank = {}
         st0 = srv.stats()
-        while nxt - t0 < args.c4_seconds:
+        t_start = time.perf_counter()
+        nxt, k, tickets = t_start, 0, []
+        rejected = 0
+        while k < len(picks) and nxt - t_start < seconds:
             now = time.perf_counter()
             if now < nxt:
-                time.sleep(min(nxt - now, 0.002))
+                if nxt - now > 0.0005:
+                    time.sleep(min(nxt - now, 0.002))
                 continue
-            cid = ids[int(rng.choice(args.c4_cubes, p=zipf_w))]
+            r = int(picks[k])
+            cam = cams[k % len(cams)]
+            out = bufs[k % len(bufs)]
+            probe = r in probe_ranks and per_rank.get(r, 0) < max_probes_per_rank
+            if probe:
+                out = np.empty(cam.nx * cam.ny, np.float32)
             try:
-                tickets.append(srv.submit(cid, cams[k % len(cams)], bufs[k % len(bufs)]))
+                t = srv.submit(ids[r], cam, out)
+                tickets.append(t)
+                if probe:
+                    per_rank[r] = per_rank.get(r, 0) + 1
+                    probes.append({"rank": r, "cam": cam, "out": out, "ticket": t, "status": None})
             except B.BirpError:
-                pass
+                rejected += 1
             k += 1
-            nxt += rng.exponential(1.0 / rate)
-        done = [r for r in (srv.wait(t, 120000) for t in tickets) if r.status == 0]
-        t1 = time.perf_counter()
+            nxt += gaps[k - 1]
+        t_offer = time.perf_counter() - t_start
+        done, lat, qms = 0, [], []
+        mine = {p["ticket"]: p for p in probes if p["status"] is None}
+        for t in tickets:
+            res = srv.wait(t, 600000)
+            if res.status == 0:
+                done += 1
+                lat.append(res.latency_ms)
+                qms.append(res.queue_ms)
+            if t in mine:
+                mine[t]["status"] = int(res.status)
+        t_all = time.perf_counter() - t_start
         st1 = srv.stats()
-        lat = np.array([r.latency_ms for r in done]) if done else np.zeros(1)
-        qms = np.array([r.queue_ms for r in done]) if done else np.zeros(1)
-        results.append({"offered_req_s": rate, "completed": len(done), "images_s": len(done) / (t1 - t0),
-                        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                        "queue_p99_ms": float(np.percentile(qms, 99)),
-                        "uploads": st1.cube_uploads - st0.cube_uploads, "evictions": st1.cube_evictions - st0.cube_evictions,
-                        "hits": st1.cube_hits - st0.cube_hits, "rejected": st1.rejected - st0.rejected})
-        print(json.dumps(results[-1]), flush=True)
+        lat = np.array(lat) if lat else np.zeros(1)
+        qms = np.array(qms) if qms else np.zeros(1)
+        return {"offered_req_s": rate, "submitted": len(tickets), "completed": done,
+                "served_images_s": done / t_all, "offer_s": t_offer, "drain_s": t_all - t_offer,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                "queue_p99_ms": float(np.percentile(qms, 99)),
+                "uploads": st1.cube_uploads - st0.cube_uploads, "evictions": st1.cube_evictions - st0.cube_evictions,
+                "rejected": rejected + (st1.rejected - st0.rejected)}
+
+    sweep = []
+    sat = 0.0
+    for rate in (float(r) for r in args.c4_rates.split(",")):
+        r = phase(rate, args.c4_seconds)
+        sweep.append(r)
+        print(json.dumps({"c4_rate": r}), file=sys.stderr, flush=True)
+        sat = max(sat, r["served_images_s"])
+        if r["served_images_s"] < 0.9 * rate:
+            break
+    saturated = bool(sweep) and sweep[-1]["served_images_s"] < 0.9 * sweep[-1]["offered_req_s"]
+    at70 = phase(0.7 * sat, 2 * args.c4_seconds, max_probes_per_rank=2) if sat > 0 else None
+    st_end = srv.stats()
     srv.close()
+    # parity of the probe images (each probe cube regenerated from its seed)
+    t0 = time.perf_counter()
+    parity = None
+    if O is not None and probes:
+        jobs, meta = [], []
+        for rank in sorted({p["rank"] for p in probes}):
+            v = synth.serving_cube(rank, bases)
+            oc = O.Cube64(xs, ys, zs, v.astype(np.float64), 1)
+            del v
+            sel = [p for p in probes if p["rank"] == rank and p["status"] == 0]
+            if sel:
+                rep = parity_report(O, [(oc, p["cam"], p["out"]) for p in sel], args.parity_px)
+                jobs += rep["per_image"]
+                meta += [rank] * len(sel)
+            del oc
+        mx = np.array([j[0] for j in jobs]) if jobs else np.zeros(1)
+        parity = {"images": len(jobs), "cube_ranks": sorted(set(meta)), "pixels_per_image": args.parity_px,
+                  "max_rel_err": float(mx.max()), "images_within_tolerance": int(np.sum(mx <= 1e-5)),
+                  "tolerance": 1e-5, "failed_requests": int(sum(1 for p in probes if p["status"] != 0)),
+                  "per_image": jobs, "check_s": time.perf_counter() - t0}
     # plain per-call latency on one resident cube of the same layout
-    cube = B.Cube(xs, ys, zs, bases[0], layout=layout)
-    for c in cams[:5]:  # untimed: the server's released pool memory is returned meanwhile
+    cube = B.Cube(xs, ys, zs, synth.serving_cube(0, bases), layout=layout)
+    for c in cams[:5]:
         B.render(cube, c, out=bufs[0][: c.nx * c.ny].reshape(c.ny, c.nx))
     pl = []
-    for c in cams[:200]:
+    for c in cams[:300]:
         t = time.perf_counter()
         B.render(cube, c, out=bufs[0][: c.nx * c.ny].reshape(c.ny, c.nx))
         pl.append(1000 * (time.perf_counter() - t))
-    print(json.dumps({"workload": f"config 4 serving sweep: {args.c4_cubes} cubes of {nx}x{ny}x{nz}, Zipf(1.1), "
-                                  f"{args.c4_budget_gb} GB budget, {args.c4_seconds} s per rate, "
-                                  f"{args.c4_layout} layout",
-                      "sweep": results, "plain_p50_ms": float(np.percentile(pl, 50)),
-                      "plain_p99_ms": float(np.percentile(pl, 99)), "plain_images_s": len(pl) / (sum(pl) / 1000)}))
+    cube_bytes = cube.info().device_bytes
+    cube.close()
+    return {"workload": f"config 4 serving sweep: {n_cubes} cubes of {nx}x{ny}x{nz} FP32 "
+                        f"({n_cubes * nx * ny * nz * 4 / 1e9:.1f} GB of pinned host copies), Zipf(1.1) popularity, "
+                        f"{args.c4_budget_gb:g} GiB device budget, {args.c4_layout} layout, Poisson arrivals, "
+                        f"{args.c4_seconds:g} s per offered rate (70% run: {2 * args.c4_seconds:g} s)",
+            "cube_device_bytes": cube_bytes,
+            "resident_cubes_in_budget": int(args.c4_budget_gb * (1 << 30) // max(cube_bytes, 1)),
+            "setup_s": setup_s, "warm_s": warm_s, "warm_uploads": int(st_warm.cube_uploads),
+            "sweep": sweep, "saturated": saturated, "saturation_images_s": sat,
+            "at_70pct_of_saturation": at70,
+            "uploads_total": int(st_end.cube_uploads), "evictions_total": int(st_end.cube_evictions),
+            "plain": {"p50_ms": float(np.percentile(pl, 50)), "p99_ms": float(np.percentile(pl, 99)),
+                      "images_s": len(pl) / (sum(pl) / 1000)},
+            "parity": parity}
+
+
+def run_profile_case(args):
+    """A small fixed batch for profiling one kernel class: the first
+    --requests requests of the orbit sampler on the 256^3 stretched cube
+    (trilinear or nearest, records or compact layout) or on the default CMEM
+    model, launched --launches times."""
+    import birp_cpp_gb300 as B
+    from birp_cpp_gb300 import build, synth
+    build.build()
+    B.init(0)
+    mode = args.profile_case
+    reqs = synth.config2_requests(args.requests, seed=2)
+    if mode == "cmem":
+        space = B.Cmem()
+    else:
+        xs, ys, zs, v = synth.cube_config1(seed=1)
+        layout = B.CUBE_COMPACT if mode == "compact" else B.CUBE_RECORDS
+        space = B.Cube(xs, ys, zs, v.astype(np.float32), layout=layout)
+    cams = [B.camera(p, a, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(s),
+                     ray_length=synth.RAY_LENGTH, trilinear=mode != "nearest") for p, a, nx, ny, s in reqs]
+    items = [(space, c) for c in cams]
+    batch = B.Batch(len(items), sum(c.nx * c.ny for c in cams))
+    for _ in range(args.launches):
+        batch.submit(items)
+        batch.wait()
+    print(json.dumps({"profile_case": mode, "requests": len(items), "last_launch_ms": batch.last_ms()[0]}))
+    batch.close()
 
 
 def cpu_sample(reqs, host, seconds: float, threads: int, seed: int = 7):
@@ -368,7 +612,7 @@ def run_reference(args, world, rank):
 
 def config_dict(args):
     return {"workload": f"{args.requests} orbit renders of a 256^3 stretched FP32 cube (config 2 on config 1's "
-                        "cube): 144x84..1024x600 px, step 0.025-0.1 Re, trilinear, PREFIX",
+                        "cube): 144x84..1024x600 px, step 0.025-0.1 Re, roll U[-10, 10] deg, trilinear, PREFIX",
             "cube": "256x256x256 stretched axes, FP32 (FP64 oracle copy)", "requests": args.requests,
             "fov_deg": [27.0, 16.0], "ray_length_re": 44.0,
             "l2": "flushed between timed steps (512 MB write); images (~445 MB) exceed L2",
@@ -385,15 +629,21 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=3.0)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--parity-px", type=int, default=256, help="pixels checked per image against the FP64 oracle")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="skip the config-3 block of the default run")
+    ap.add_argument("--no-c4", action="store_true", help="skip the config-4 block of the default run")
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
-                    help="c2: the 512-request single-cube batch (default); c3: 48-cube + CMEM batch; "
-                         "c4: serving sweep")
-    ap.add_argument("--c4-cubes", type=int, default=64)
+                    help="c2: the default run (headline on config 2, plus the c3 and c4 blocks); c3 / c4: that "
+                         "block alone")
+    ap.add_argument("--profile-case", choices=["trilinear", "nearest", "compact", "cmem"],
+                    help="run a small fixed batch of one kernel class (for a profiler) and exit")
+    ap.add_argument("--launches", type=int, default=4, help="launches of --profile-case")
+    ap.add_argument("--c4-cubes", type=int, default=256)
     ap.add_argument("--c4-dims", default="512x384x384")
     ap.add_argument("--c4-budget-gb", type=float, default=60.0)
-    ap.add_argument("--c4-rates", default="50,200,500,1000,2000")
-    ap.add_argument("--c4-seconds", type=float, default=10.0)
+    ap.add_argument("--c4-rates", default="50,200,500,1000,2000,3000,4000,6000,8000,12000,16000")
+    ap.add_argument("--c4-seconds", type=float, default=4.0)
     ap.add_argument("--c4-layout", default="compact", choices=["compact", "records"],
                     help="device layout of the served cubes")
     args = ap.parse_args()
@@ -401,13 +651,27 @@ def main():
     if args.impl == "reference":
         run_reference(args, world, rank)
         return
-    if args.workload in ("c3", "c4"):
-        import birp_cpp_gb300 as B
-        (run_c3 if args.workload == "c3" else run_c4)(args, B)
+    if args.profile_case:
+        if args.requests == 512:
+            args.requests = 64
+        run_profile_case(args)
         return
-
     import birp_cpp_gb300 as B
     from birp_cpp_gb300 import build
+    if args.workload in ("c3", "c4"):
+        O = oracle()
+        host_c3 = gen_c3_host() if args.workload == "c3" else None
+        build.build()
+        B.init(0)
+        out = run_c3(args, B, O, *host_c3) if args.workload == "c3" else run_c4(args, B, O)
+        print(json.dumps(out))
+        return
+
+    extra_blocks = world == 1 and rank == 0
+    # the oracle is built, and config 3's cubes generated in spawned
+    # processes, before the first GPU call
+    O = oracle() if rank == 0 else None
+    host_c3 = gen_c3_host() if extra_blocks and not args.no_c3 else None
     build.build()
     B.init(local)
     W = make_workload(B, args.requests)
@@ -464,8 +728,15 @@ def main():
     e2e_breakdown = {"kernel_ms": k_mean, "d2h_ms": t_mean - k_mean,
                      "host_ms": float(np.mean(e2e_t)) * 1e3 - t_mean}
 
-    # ---- parity spot check of the timed images against the FP64 oracle
-    parity = spot_check(W, outs) if rank == 0 else None
+    # ---- parity of every timed image against the FP64 oracle
+    parity = None
+    if rank == 0:
+        xs, ys, zs, v32 = W["host"]
+        oc = O.Cube64(xs, ys, zs, v32.astype(np.float64), 1)
+        parity = parity_report(O, [(oc, c, o) for c, o in zip(cams, outs)], args.parity_px,
+                               label="every image of the last e2e step, a random pixel sample each")
+        parity["full_images"] = full_image_checks(O, oc, cams, outs)
+        del oc
 
     # ---- plain per-call path on the same requests
     plain = None
@@ -504,7 +775,7 @@ def main():
                                           "batched_vs_plain": bi / pi}
 
     # ---- roofline of the batched kernel (measured peaks)
-    fp32_tflops, l2_gbs = B.measure_peaks()
+    fp32_tflops, l2_gbs, l2_buf = B.measure_peaks()
     t_k = step_ms / 1000.0
     cells_per_step = ks["cells"] / args.steps
 
@@ -521,7 +792,9 @@ def main():
     roofline = roof(cells_per_step, FLOP_PER_CELL, BYTES_PER_CELL,
                     f"{cells_per_step:.4g} cell segments/launch x {FLOP_PER_CELL:.0f} flop, {BYTES_PER_CELL:.0f} B")
     roofline.update({"traffic": traffic_from_profile(), "kernel": "render_batch_kernel",
-                     "peak_source": "measured in-run: FP32 FMA loop and L2-resident read (birp_measure_peaks)",
+                     "peak_source": f"measured in-run: FP32 FMA loop and L2-resident read (birp_measure_peaks: "
+                                    f"loads that bypass L1, best of 16, 32 and 64 MB buffers, set by the "
+                                    f"{l2_buf >> 20} MB one)",
                      "fp32_frac": cells_per_step * FLOP_PER_CELL / t_k / 1e12 / fp32_tflops,
                      "l2_frac": cells_per_step * BYTES_PER_CELL / t_k / 1e9 / l2_gbs})
     # the kernel is bound by instruction issue: warp instructions per cell
@@ -565,14 +838,25 @@ def main():
         v, px, t = cpu_sample(W["reqs"], W["host"], args.cpu_seconds, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{px} random pixels of the {args.requests}-request workload, {t:.1f} s on {threads} "
-                         f"threads; images/s extrapolated by total pixels"}
+                         f"threads; images/s extrapolated by total pixels (the reference has no roll input; the "
+                         f"cost of a pixel does not depend on it)"}
         v1, px1, t1 = cpu_sample(W["reqs"], W["host"], max(2.0, args.cpu_seconds / 3), 1, seed=11)
         cpu["single_core"] = {"value": v1, "unit": UNIT, "cores": 1,
                               "sample": f"{px1} random pixels, {t1:.1f} s on 1 thread"}
+    clock_summary = clocks.summary()
+    h2d = batch.upload_bytes()  # request descriptors and work tables, copied each step
+    batch.close()
+    cube.close()
+
+    # ---- the config-3 and config-4 blocks (one GPU only)
+    c3 = c4 = None
+    if extra_blocks and host_c3 is not None:
+        c3 = run_c3(args, B, O, *host_c3)
+        del host_c3
+    if extra_blocks and not args.no_c4:
+        c4 = run_c4(args, B, O)
 
     if rank == 0:
-        h2d = batch.upload_bytes()  # request descriptors and work tables, copied each step
-        clock_summary = clocks.summary()
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -588,41 +872,17 @@ def main():
             "roofline": roofline, "roofline_issue": issue_roofline(clock_summary.get("sm_mhz")),
             "roofline_per_sample": roofline_per_sample,
             "roofline_hbm": roofline_hbm,
-            "cpu_baseline": cpu, "parity": parity,
+            "cpu_baseline": cpu,
             # each step replays one graph with four kernels: the CMEM, nearest
             # and compact-layout ones (no work here) and the records-layout
             # trilinear one
             "gpu_launches": 4 * args.steps, "clocks": clock_summary,
             "exact_fp64_rays_per_step": ks["exact_range_rays"] / args.steps,
             "samples_per_cell": (ks["samples"] / ks["cells"]) if ks.get("cells") else None,
+            "c3": c3, "c4": c4,
+            "parity": parity,
         }
         print(json.dumps(line))
-
-
-def spot_check(W, outs, n_pix: int = 3000):
-    """Max/RMS relative error of random pixels of the timed images against the
-    FP64 oracle."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pyoracle as O
-    from birp_cpp_gb300 import synth
-    O.build()
-    xs, ys, zs, v32 = W["host"]
-    oc = O.Cube64(xs, ys, zs, v32.astype(np.float64), 1)
-    rng = np.random.default_rng(5)
-    errs = []
-    for r in rng.choice(len(W["reqs"]), 8, replace=False):
-        pos, aim, nx, ny, step = W["reqs"][r]
-        cam = O.camera64(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, synth.n_samples(step), synth.RAY_LENGTH, 0)
-        pi = rng.integers(0, nx, n_pix // 8)
-        pj = rng.integers(0, ny, n_pix // 8)
-        ref = O.render64_pixels(oc, cam, pi, pj, threads=os.cpu_count() or 4)
-        got = outs[r][pj, pi].astype(np.float64)
-        m = ref > 1e-3 * max(ref.max(), 1e-300)
-        if m.any():
-            errs.append(np.abs(got[m] - ref[m]) / ref[m])
-    e = np.concatenate(errs) if errs else np.zeros(1)
-    return {"max_rel_err": float(e.max()), "rms_rel_err": float(np.sqrt(np.mean(e * e))), "pixels": int(e.size),
-            "tolerance": 1e-5}
 
 
 def serve_latency(B, W, rate: float, seconds: float, seed: int = 13):

@@ -1555,7 +1555,8 @@ __global__ void cmem_radii_check_kernel(const CmemDev* __restrict__ cmem, int n,
 }
 
 // Peak probes for the roofline denominators: an FP32 FMA loop (8 independent
-// chains per thread) and a read of an L2-resident buffer.
+// chains per thread) and a read of an L2-resident buffer with loads cached in
+// L2 only (ld.global.cg), so the rate is the L2's, not L1 hits.
 __global__ void peak_fp32_kernel(float* sink, int iters) {
   float a = 0.999f, b = 1e-3f;
   float x0 = threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
@@ -1572,7 +1573,7 @@ __global__ void peak_read_kernel(const float4* __restrict__ buf, size_t n4, int 
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (int r = 0; r < reps; ++r)
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += stride) {
-      float4 v = __ldg(buf + i);
+      float4 v = __ldcg(buf + i);
       acc += v.x + v.y + v.z + v.w;
     }
   if (acc == 1234.5f) sink[0] = acc;

@@ -3,10 +3,17 @@
 # where they lie (src/Camera.cpp, DataCube.cpp, Cmem.cpp, Helper.cpp), plus
 # the no-op EleFits headers in oracle/ref_shim and the C wrappers
 # oracle/ref_capi.cpp and oracle/helper_shim.cpp. Test infrastructure only (pins the oracle and makes the
-# golden fixtures); the reference tree exists only in the development
-# container, so this is skipped elsewhere.
+# golden fixtures).
+#
+# Usage: build_ref.sh <reference project directory>   (or BIRP_REFERENCE_DIR=<dir>)
+# Without a directory that holds the reference sources it builds nothing and
+# exits 0, so a machine without the reference tree skips it.
 set -e
-REF=${BIRP_REFERENCE_DIR:-/root/reference}
+REF=${1:-$BIRP_REFERENCE_DIR}
+if [ -z "$REF" ]; then
+  echo "no reference directory given (argument or BIRP_REFERENCE_DIR); skipping oracle/_ref" >&2
+  exit 0
+fi
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/src/Camera.cpp" ]; then

@@ -1,8 +1,8 @@
 """Generates the golden fixtures in tests/golden/ by running the UNMODIFIED
 reference renderer, built from its own sources by oracle/build_ref.sh.
 
-Run in a tree where the reference sources exist:
-    python tests/golden/make_golden.py
+Run with the reference project's directory (or BIRP_REFERENCE_DIR set):
+    python tests/golden/make_golden.py <reference project directory>
 The fixtures pin the oracle restatement (oracle/birp_oracle.cpp) bit for bit;
 the tests never need the reference itself. Inputs are seeded, so rerunning
 reproduces the files exactly.
@@ -61,7 +61,8 @@ def small_cube(rng):
 
 
 def main():
-    r = subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh")], capture_output=True, text=True)
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BIRP_REFERENCE_DIR", "")
+    r = subprocess.run([os.path.join(ROOT, "oracle", "build_ref.sh"), ref_dir], capture_output=True, text=True)
     if r.returncode != 0 or not os.path.exists(O.REF_PATH):
         sys.exit("reference build unavailable: " + r.stdout + r.stderr)
     R = O.Reference()
