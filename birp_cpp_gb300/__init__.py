@@ -127,6 +127,7 @@ def lib():
             "birp_cmem_margin_check": ([P, I, P, P], I),
             "birp_flush_l2": ([], I),
             "birp_measure_peaks": ([P, P, P], I),
+            "birp_fastmath_check": ([I, P, P, I, P, P], I),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -293,6 +294,17 @@ def kernel_stats(reset: bool = False) -> dict:
 
 def flush_l2() -> None:
     check(lib().birp_flush_l2())
+
+
+def fastmath_check(which: int, x, y=None):
+    """(fast, library) values of one of the CMEM kernel's fast functions on the
+    GPU at the FP32 arguments x (and y): 0 atan2_pos(y, x), 1 pow_pos(x, y),
+    2 sqrt_fast(x), 3 ex2_fast(x) (birp_fastmath_check)."""
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.ascontiguousarray(np.zeros_like(x) if y is None else y, np.float32)
+    fast, libv = np.empty_like(x), np.empty_like(x)
+    check(lib().birp_fastmath_check(int(which), _p(x), _p(y), len(x), _p(fast), _p(libv)))
+    return fast, libv
 
 
 def measure_peaks() -> tuple[float, float, int]:

@@ -38,8 +38,12 @@ static void free_batch(birp_batch* b) {
   if (b->d_stage) cudaFree(b->d_stage);
   if (b->d_out) cudaFree(b->d_out);
   if (b->d_counter) cudaFree(b->d_counter);
-  for (cudaEvent_t e : {b->e_start, b->e_kernel, b->e_end})
+  for (cudaEvent_t e : {b->e_start, b->e_kernel, b->e_end, b->fork})
     if (e) cudaEventDestroy(e);
+  for (int c = 0; c < BATCH_CLASSES; ++c) {
+    if (b->join[c]) cudaEventDestroy(b->join[c]);
+    if (b->branch[c]) cudaStreamDestroy(b->branch[c]);
+  }
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
 }
@@ -76,18 +80,27 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
       (e = cudaMalloc(&b->d_out, (size_t)max_pixels * sizeof(float))) != cudaSuccess ||
       (e = cudaHostAlloc(&b->h_out, (size_t)max_pixels * sizeof(float), cudaHostAllocDefault)) != cudaSuccess ||
       (e = cudaEventCreate(&b->e_start)) != cudaSuccess || (e = cudaEventCreate(&b->e_kernel)) != cudaSuccess ||
-      (e = cudaEventCreate(&b->e_end)) != cudaSuccess)
+      (e = cudaEventCreate(&b->e_end)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess)
     return bail(fail(e == cudaErrorMemoryAllocation ? BIRP_ERR_NOMEM : BIRP_ERR_CUDA, "batch allocation: %s",
                      cudaGetErrorString(e)));
+  for (int c = 0; c < BATCH_CLASSES; ++c)
+    if ((e = cudaStreamCreateWithFlags(&b->branch[c], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->join[c], cudaEventDisableTiming)) != cudaSuccess)
+      return bail(fail(BIRP_ERR_CUDA, "batch streams: %s", cudaGetErrorString(e)));
   std::memset(b->h_stage, 0, b->stage_bytes);
 
-  // One graph: descriptors H2D, the queue heads reset, then the CMEM kernel
-  // (few but heavy requests, so they start first), the nearest-mode kernel
-  // and the two trilinear-cube kernels (compact, then records layout; 64
-  // registers, full occupancy). A class with no requests costs one launch
-  // whose CTAs exit at once; every request falls in one of these classes, so
-  // the general kernel is not launched.
-  BatchDev bd[BATCH_CLASSES];
+  // One graph: descriptors H2D, the queue heads reset, then the kernels of
+  // the four classes as parallel branches: CMEM (few but heavy requests),
+  // nearest mode, and the two trilinear-cube kernels (compact and records
+  // layout). Each is a persistent kernel sized to fill the GPU on its own;
+  // launched side by side, the CTAs of one class take the SM slots that
+  // another class's CTAs leave when its queue runs dry, so the classes of a
+  // mixed batch overlap instead of each paying its tail in turn, and a class
+  // with no requests (its CTAs exit at once) costs no serial launch gap.
+  // Every request falls in one of these classes, so the general kernel is not
+  // launched.
+  BatchDev* bd = b->bd;
   for (int c = 0; c < BATCH_CLASSES; ++c) {
     bd[c].hdr = reinterpret_cast<const int*>(b->d_stage) + 4 * c;
     bd[c].first = reinterpret_cast<const int*>(b->d_stage + b->off_first[c]);
@@ -101,12 +114,34 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
     return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
   cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
   cudaMemsetAsync(b->d_counter, 0, BATCH_CLASSES * sizeof(unsigned int), b->stream);
-  for (int c : {BATCH_CMEM, BATCH_CUBE_NEAREST, BATCH_CUBE_TRI_COMPACT, BATCH_CUBE_TRI})
-    launch_render_batch(bd[c], b->grid[c], b->stream, c);
+  cudaEventRecord(b->fork, b->stream);
+  for (int c : {BATCH_CMEM, BATCH_CUBE_NEAREST, BATCH_CUBE_TRI_COMPACT, BATCH_CUBE_TRI}) {
+    cudaStreamWaitEvent(b->branch[c], b->fork, 0);
+    launch_render_batch(bd[c], b->grid[c], b->branch[c], c);
+    cudaEventRecord(b->join[c], b->branch[c]);
+    cudaStreamWaitEvent(b->stream, b->join[c], 0);
+  }
   e = cudaStreamEndCapture(b->stream, &b->graph);
   if (e != cudaSuccess) return bail(fail(BIRP_ERR_CUDA, "capture: %s", cudaGetErrorString(e)));
   if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess)
     return bail(fail(BIRP_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e)));
+  // the CMEM kernel's node, whose model parameter each launch may set
+  size_t n_nodes = 0;
+  if ((e = cudaGraphGetNodes(b->graph, nullptr, &n_nodes)) != cudaSuccess)
+    return bail(fail(BIRP_ERR_CUDA, "graph nodes: %s", cudaGetErrorString(e)));
+  std::vector<cudaGraphNode_t> nodes(n_nodes);
+  if ((e = cudaGraphGetNodes(b->graph, nodes.data(), &n_nodes)) != cudaSuccess)
+    return bail(fail(BIRP_ERR_CUDA, "graph nodes: %s", cudaGetErrorString(e)));
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    cudaKernelNodeParams kp{};
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel &&
+        cudaGraphKernelNodeGetParams(nd, &kp) == cudaSuccess && kp.func == render_batch_function(BATCH_CMEM)) {
+      b->cmem_node = nd;
+      b->cmem_launch = kp;
+    }
+  }
+  if (!b->cmem_node) return bail(fail(BIRP_ERR_CUDA, "batch graph without its CMEM kernel node"));
   *out = b;
   return ok();
 }
@@ -153,6 +188,29 @@ birp_status batch_submit(birp_batch* b, const birp_request* reqs, int n, float* 
     }
     hdr[4 * cls] = k;
     hdr[4 * cls + 1] = first[k];
+  }
+  // one CMEM model for every CMEM request: the CMEM kernel gets it as a
+  // parameter (its constants become operands instead of loads)
+  const birp_cmem* model = nullptr;
+  bool one_model = true;
+  for (int i = 0; i < n; ++i)
+    if (reqs[i].cmem) {
+      if (!model) model = reqs[i].cmem;
+      else if (reqs[i].cmem != model) one_model = false;
+    }
+  CmemParam cp{};
+  if (model && one_model) {
+    cp.m = model->h_desc;
+    cp.dev = model->d_desc;
+  }
+  if (std::memcmp(&cp, &b->cmem_model, sizeof cp) != 0) {
+    cudaKernelNodeParams kp = b->cmem_launch;
+    void* args[2] = {&b->bd[BATCH_CMEM], &cp};
+    kp.kernelParams = args;
+    kp.extra = nullptr;
+    cudaError_t e = cudaGraphExecKernelNodeSetParams(b->exec, b->cmem_node, &kp);
+    if (e != cudaSuccess) return fail(BIRP_ERR_CUDA, "CMEM model parameter: %s", cudaGetErrorString(e));
+    b->cmem_model = cp;
   }
   b->n = n;
   b->used = used;

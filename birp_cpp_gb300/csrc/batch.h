@@ -25,9 +25,20 @@ struct birp_batch {
   bool pending = false;
   bool direct = false;       // the last launch wrote the caller's host images itself
   cudaStream_t stream = nullptr;
-  // {descriptors H2D, queue heads reset, the kernels of the classes}
+  // capture-time streams and events of the graph's parallel branches (one
+  // branch per kernel class)
+  cudaStream_t branch[birp::BATCH_CLASSES] = {};
+  cudaEvent_t fork = nullptr, join[birp::BATCH_CLASSES] = {};
+  // {descriptors H2D, queue heads reset, then the kernels of the classes as
+  // parallel branches}
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  birp::BatchDev bd[birp::BATCH_CLASSES] = {};  // the kernels' work tables
+  // the CMEM class kernel's node: its CMEM model parameter is set before a
+  // launch whose CMEM requests share one model
+  cudaGraphNode_t cmem_node = nullptr;
+  cudaKernelNodeParams cmem_launch{};
+  birp::CmemParam cmem_model{};  // the parameter the node holds now
   cudaEvent_t e_start = nullptr, e_kernel = nullptr, e_end = nullptr;
 };
 

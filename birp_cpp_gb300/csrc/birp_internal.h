@@ -99,6 +99,15 @@ struct CmemDev {
   float eps_rel;  // FP32 boundary-decision margin (relative to r)
 };
 
+// A CMEM model passed by value as a kernel parameter: the kernels that take
+// one read its constants as parameter operands (no loads) for the requests
+// whose model is `dev`; other requests (dev == nullptr: all) read theirs
+// through RequestDev::cmem.
+struct CmemParam {
+  CmemDev m;
+  const CmemDev* dev;
+};
+
 enum SpaceKind : int { SPACE_CUBE = 0, SPACE_CMEM = 1 };
 enum MarchMode : int { MARCH_PREFIX = 0, MARCH_CLIP = 1 };
 
@@ -154,7 +163,10 @@ struct BatchDev {
 };
 
 // Host-side launch helpers (render.cu).
-cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaStream_t stream);
+// cmem_host: the host copy of req's CMEM model (CMEM requests), passed to the
+// kernel as a parameter
+cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaStream_t stream,
+                                const CmemDev* cmem_host = nullptr);
 // Persistent batch kernel classes: CUBE_TRI renders only trilinear cube
 // requests (fewer registers, more resident warps); ANY renders every kind.
 // Persistent-kernel classes: trilinear cube requests in the records layout,
@@ -169,7 +181,13 @@ enum BatchClass : int {
   BATCH_CUBE_NEAREST = 4,
   BATCH_CLASSES = 5
 };
-cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY);
+// model: the CMEM model the CMEM class kernel takes as a parameter (nullptr:
+// none, every request reads its model through its pointer)
+cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream, int cls = BATCH_ANY,
+                                const CmemParam* model = nullptr);
+// The persistent kernel of class cls (its launch's function, for finding its
+// node in a captured graph).
+const void* render_batch_function(int cls);
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
 cudaError_t launch_cube_negflags(const float* padded, int nx, int ny, int nz, uint8_t* flags, cudaStream_t stream);
@@ -184,6 +202,9 @@ cudaError_t launch_cmem_sample(const CmemDev* cmem, const float* xyz, int n, flo
 cudaError_t launch_cmem_radii_check(const CmemDev* cmem, int n, unsigned long long seed, float* max_err,
                                     cudaStream_t stream);
 cudaError_t launch_peak_fp32(float* sink, int blocks, int iters, cudaStream_t stream);
+// the CMEM kernel's fast functions beside CUDA's (see birp_fastmath_check)
+cudaError_t launch_fastmath(int which, const float* x, const float* y, int n, float* fast, float* lib,
+                            cudaStream_t stream);
 cudaError_t launch_peak_read(const float4* buf, size_t n4, int reps, float* sink, int blocks, cudaStream_t stream);
 int tile_w(int seg_log2);
 int tile_h(int seg_log2);

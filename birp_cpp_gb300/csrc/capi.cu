@@ -528,6 +528,25 @@ birp_status birp_cmem_margin_check(const birp_cmem* m, int n, float* max_rel_err
   return ok();
 }
 
+birp_status birp_fastmath_check(int which, const float* x, const float* y, int n, float* fast, float* lib) {
+  if (birp_status s = check_init()) return s;
+  if (which < 0 || which > 3 || n < 0 || (n > 0 && (!x || !y || !fast || !lib)))
+    return fail(BIRP_ERR_INVALID, "bad argument");
+  if (n == 0) return ok();
+  std::lock_guard<std::mutex> lk(g_ctx.mu);
+  if (birp_status s = ensure_xyz_scratch((size_t)n * 4)) return s;
+  float* dx = g_ctx.xyz_scratch;
+  float *dy = dx + n, *df = dx + 2 * (size_t)n, *dl = dx + 3 * (size_t)n;
+  cudaStream_t st = g_ctx.stream;
+  CK(cudaMemcpyAsync(dx, x, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(dy, y, sizeof(float) * n, cudaMemcpyHostToDevice, st));
+  CK(launch_fastmath(which, dx, dy, n, df, dl, st));
+  CK(cudaMemcpyAsync(fast, df, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(lib, dl, sizeof(float) * n, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return ok();
+}
+
 // ---------------------------------------------------------------- camera / render
 
 void birp_camera_defaults(birp_camera* c) {
@@ -570,7 +589,7 @@ birp_status birp_render_device(const birp_cube* cube, const birp_cmem* cmem, con
   if (!out_device) return fail(BIRP_ERR_INVALID, "out_device is NULL");
   RequestDev r;
   if (birp_status s = build_request(cube, cmem, *cam, out_device, r)) return s;
-  CK(launch_render_plain(r, g_ctx.stats, pick_stream(stream)));
+  CK(launch_render_plain(r, g_ctx.stats, pick_stream(stream), cmem ? &cmem->h_desc : nullptr));
   return ok();
 }
 
@@ -587,11 +606,11 @@ birp_status birp_render(const birp_cube* cube, const birp_cmem* cmem, const birp
     // the kernel writes every pixel of the caller's image itself
     if (birp_status s = build_request(cube, cmem, *cam, out_host, r)) return s;
     prefault_outputs(&out_host, &npx, 1);
-    CK(launch_render_plain(r, g_ctx.stats, st));
+    CK(launch_render_plain(r, g_ctx.stats, st, cmem ? &cmem->h_desc : nullptr));
   } else {
     if (birp_status s = ensure_scratch(npx)) return s;
     if (birp_status s = build_request(cube, cmem, *cam, g_ctx.scratch, r)) return s;
-    CK(launch_render_plain(r, g_ctx.stats, st));
+    CK(launch_render_plain(r, g_ctx.stats, st, cmem ? &cmem->h_desc : nullptr));
     CK(cudaMemcpyAsync(out_host, g_ctx.scratch, npx * sizeof(float), cudaMemcpyDeviceToHost, st));
   }
   CK(cudaStreamSynchronize(st));
@@ -614,7 +633,7 @@ birp_status birp_time_render_device(const birp_cube* cube, const birp_cmem* cmem
   for (int i = 0; i < repeats; ++i) {
     if (flush_l2) CK(cudaMemsetAsync(g_ctx.flush, i & 0xff, flush_bytes, st));
     CK(cudaEventRecord(e0, st));
-    CK(launch_render_plain(r, g_ctx.stats, st));
+    CK(launch_render_plain(r, g_ctx.stats, st, cmem ? &cmem->h_desc : nullptr));
     CK(cudaEventRecord(e1, st));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;

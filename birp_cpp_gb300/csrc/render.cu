@@ -285,22 +285,23 @@ __device__ __forceinline__ float rsqrt_fast(float x) {
 }
 
 // atan2(y, x) for y >= 0 (result in [0, pi]; not both 0). With a = min/max
-// of (|x|, y) in [0, 1], atan(a) = a P(a^2) with P of degree 8, fitted for
-// this function by iteratively reweighted least squares toward the minimax
-// absolute error on 4000 Chebyshev nodes of a^2 in [0, 1] (largest error
-// 8.4e-8 rad evaluated in FP32); then atan(y/|x|) = pi/2 - atan(|x|/y) when
-// y > |x|, and pi - atan(y/|x|) when x < 0. Error <= ~2.5e-7 rad with the
-// hardware-reciprocal division.
+// of (|x|, y) in [0, 1], atan(a) = a P(a^2) with P of degree 8: the minimax
+// polynomial of the absolute error on 4000 Chebyshev nodes of a^2 in [0, 1]
+// (Lawson's iteratively reweighted least squares in FP64, rounded once to
+// FP32; tests/fit_atan2.py regenerates these lines; largest error 9.8e-8 rad
+// evaluated in FP32); then atan(y/|x|) = pi/2 - atan(|x|/y) when y > |x|, and
+// pi - atan(y/|x|) when x < 0. Error <= ~3e-7 rad with the hardware-reciprocal
+// division (checked against atan2f on the GPU by tests/test_gpu_fastmath.py).
 __device__ __forceinline__ float atan2_pos(float y, float x) {
   const float ax = fabsf(x);
   const float a = __fdividef(fminf(ax, y), fmaxf(ax, y));
   const float s = a * a;
-  float p = 0.00245668f;
-  p = fmaf(p, s, -0.01440118f);
-  p = fmaf(p, s, 0.03978092f);
-  p = fmaf(p, s, -0.07234829f);
-  p = fmaf(p, s, 0.10498931f);
-  p = fmaf(p, s, -0.14161225f);
+  float p = 0.0024567256f;
+  p = fmaf(p, s, -0.014401361f);
+  p = fmaf(p, s, 0.03978123f);
+  p = fmaf(p, s, -0.07234858f);
+  p = fmaf(p, s, 0.10498946f);
+  p = fmaf(p, s, -0.14161229f);
   p = fmaf(p, s, 0.19985907f);
   p = fmaf(p, s, -0.33332598f);
   p = fmaf(p, s, 0.9999999f);
@@ -610,9 +611,11 @@ enum Axes { AXES_NONE = 0, AXES_DDA = 2, AXES_DDA_COMPACT = 3 };
 // One pixel tile of one request. The lanes-per-ray split S = 2^seg_log2 is a
 // runtime value of the request (it only sets the tile shape, the lane -> ray
 // map, the sample stride and the merge); the march itself is S-independent.
+// P: a CMEM model passed as a kernel parameter (nullptr: none); CMEM
+// requests whose model it is read its constants from the parameter space.
 template <int KIND, int INTERP, int AXES>
 __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty, TileSmem& sm,
-                                            KernelStats* stats) {
+                                            KernelStats* stats, const CmemParam* P = nullptr) {
   const int SEGL2 = R.seg_log2;
   const int S = 1 << SEGL2;
   const int WBX = wb_x(SEGL2), WBY = wb_y(SEGL2);
@@ -1238,7 +1241,6 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     }
     n_exact_nearest = n_fp64;
   } else {
-    const CmemDev& M = *R.cmem;
     float st[3], bs[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -1249,21 +1251,27 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     const float apos = fabsf(R.pos32[0]) + fabsf(R.pos32[1]) + fabsf(R.pos32[2]);
     const float perr_slope = R.dt32 * (kDirErr + 5e-7f);
     const float perr_base = 0.5f * perr_slope + apos * 5e-7f + 1e-6f;
+    auto march = [&](const CmemDev& M) {
 #pragma unroll 1
-    for (int it = 0; it < iters; ++it) {
-      float x = fmaf(fi, st[0], bs[0]), y = fmaf(fi, st[1], bs[1]), z = fmaf(fi, st[2], bs[2]);
-      CmemEval e = cmem_value32(M, x, y, z, fmaf(fi, perr_slope, perr_base));
-      float v = e.v;
-      if (e.unsure) {
-        need_d64();
-        int i = first + (it << SEGL2);
-        v = (float)cmem_value64(M, pos64(R.pos[0], d64[0], R.dt, i), pos64(R.pos[1], d64[1], R.dt, i),
-                                pos64(R.pos[2], d64[2], R.dt, i));
-        if (stats) atomicAdd(&stats->exact_cmem, 1ull);
+      for (int it = 0; it < iters; ++it) {
+        float x = fmaf(fi, st[0], bs[0]), y = fmaf(fi, st[1], bs[1]), z = fmaf(fi, st[2], bs[2]);
+        CmemEval e = cmem_value32(M, x, y, z, fmaf(fi, perr_slope, perr_base));
+        float v = e.v;
+        if (e.unsure) {
+          need_d64();
+          int i = first + (it << SEGL2);
+          v = (float)cmem_value64(M, pos64(R.pos[0], d64[0], R.dt, i), pos64(R.pos[1], d64[1], R.dt, i),
+                                  pos64(R.pos[2], d64[2], R.dt, i));
+          if (stats) atomicAdd(&stats->exact_cmem, 1ull);
+        }
+        acc.add(v);
+        fi += fS;
       }
-      acc.add(v);
-      fi += fS;
-    }
+    };
+    // the model's constants as parameter operands where the kernel was given
+    // this request's model (one uniform branch per tile), else loaded
+    if (P != nullptr && R.cmem == P->dev) march(P->m);
+    else march(*R.cmem);
   }
 
   if (stats) {
@@ -1291,11 +1299,13 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 }
 
 // One request, one CTA per tile; the request travels as a kernel parameter.
+// CMEM requests also get their model as a parameter.
 template <int KIND, int INTERP, int AXES>
 __global__ void __launch_bounds__(kThreads) render_plain_kernel(const __grid_constant__ RequestDev req,
+                                                                const __grid_constant__ CmemParam model,
                                                                 KernelStats* stats) {
   __shared__ TileSmem sm;
-  render_tile<KIND, INTERP, AXES>(req, blockIdx.x, blockIdx.y, sm, stats);
+  render_tile<KIND, INTERP, AXES>(req, blockIdx.x, blockIdx.y, sm, stats, KIND == SPACE_CMEM ? &model : nullptr);
 }
 
 // Dispatch over the request's variant.
@@ -1317,13 +1327,15 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
 // queue is empty. Items are numbered in the host's order (largest work
 // first). CLS = BATCH_CUBE_TRI compiles only the trilinear cube march (fewer
 // registers, more resident warps); BATCH_ANY renders every request kind.
+// `model`: the CMEM class kernel reads this CMEM model's constants as
+// parameter operands for the requests that use it (model.dev).
 template <int CLS>
 __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
                                            : CLS == BATCH_CMEM         ? BIRP_CMEM_MINB
                                            : CLS == BATCH_CUBE_NEAREST ? BIRP_NEAREST_MINB
                                            : CLS == BATCH_CUBE_TRI_COMPACT ? BIRP_COMPACT_MINB
                                                                        : BIRP_WALK_MINB)
-    render_batch_kernel(BatchDev B) {
+    render_batch_kernel(BatchDev B, const __grid_constant__ CmemParam model) {
   __shared__ TileSmem sm;
   __shared__ int s_item;
   const int n_reqs = __ldg(B.hdr), total_items = __ldg(B.hdr + 1);
@@ -1349,7 +1361,7 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
     } else if constexpr (CLS == BATCH_CUBE_TRI_COMPACT) {
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CMEM) {
-      render_tile<SPACE_CMEM, TRILINEAR, AXES_NONE>(R, tx, ty, sm, B.stats);
+      render_tile<SPACE_CMEM, TRILINEAR, AXES_NONE>(R, tx, ty, sm, B.stats, &model);
     } else if constexpr (CLS == BATCH_CUBE_NEAREST) {
       if (R.compact) render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
       else render_tile<SPACE_CUBE, NEAREST, AXES_DDA>(R, tx, ty, sm, B.stats);
@@ -1554,6 +1566,32 @@ __global__ void cmem_radii_check_kernel(const CmemDev* __restrict__ cmem, int n,
   atomicMax(reinterpret_cast<unsigned int*>(max_err), __float_as_uint(worst));
 }
 
+// The CMEM kernel's one-instruction and polynomial functions beside CUDA's
+// own, at the same FP32 arguments: which = 0 atan2_pos(y, x) / atan2f,
+// 1 pow_pos(x, y) / powf, 2 sqrt_fast(x) / sqrtf, 3 ex2_fast(x) / exp2f.
+__global__ void fastmath_kernel(int which, const float* __restrict__ x, const float* __restrict__ y, int n,
+                                float* __restrict__ fast, float* __restrict__ lib) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const float a = x[t], b = y[t];
+    float f, l;
+    if (which == 0) {
+      f = atan2_pos(b, a);
+      l = atan2f(b, a);
+    } else if (which == 1) {
+      f = pow_pos(a, b);
+      l = powf(a, b);
+    } else if (which == 2) {
+      f = sqrt_fast(a);
+      l = sqrtf(a);
+    } else {
+      f = ex2_fast(a);
+      l = exp2f(a);
+    }
+    fast[t] = f;
+    lib[t] = l;
+  }
+}
+
 // Peak probes for the roofline denominators: an FP32 FMA loop (8 independent
 // chains per thread) and a read of an L2-resident buffer with loads cached in
 // L2 only (ld.global.cg), so the rate is the L2's, not L1 hits.
@@ -1581,6 +1619,13 @@ __global__ void peak_read_kernel(const float4* __restrict__ buf, size_t n4, int 
 
 }  // namespace
 
+cudaError_t launch_fastmath(int which, const float* x, const float* y, int n, float* fast, float* lib,
+                            cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  fastmath_kernel<<<std::min((n + 255) / 256, 4096), 256, 0, s>>>(which, x, y, n, fast, lib);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_peak_fp32(float* sink, int blocks, int iters, cudaStream_t s) {
   peak_fp32_kernel<<<blocks, 256, 0, s>>>(sink, iters);
   return cudaGetLastError();
@@ -1594,14 +1639,19 @@ cudaError_t launch_peak_read(const float4* buf, size_t n4, int reps, float* sink
 int tile_w(int segl2) { return tw_of(segl2); }
 int tile_h(int segl2) { return th_of(segl2); }
 
-cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStream_t s) {
+cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStream_t s, const CmemDev* cmem_host) {
   dim3 grid((h.nx + tw_of(h.seg_log2) - 1) / tw_of(h.seg_log2), (h.ny + th_of(h.seg_log2) - 1) / th_of(h.seg_log2));
-  if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_NONE><<<grid, kThreads, 0, s>>>(h, stats);
+  CmemParam cp{};
+  if (h.kind == SPACE_CMEM && cmem_host) {
+    cp.m = *cmem_host;
+    cp.dev = h.cmem;
+  }
+  if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_NONE><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.interp && h.compact)
-    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, stats);
-  else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, stats);
-  else if (h.compact) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, stats);
-  else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA><<<grid, kThreads, 0, s>>>(h, stats);
+    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else if (h.compact) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA><<<grid, kThreads, 0, s>>>(h, cp, stats);
   return cudaGetLastError();
 }
 
@@ -1623,13 +1673,23 @@ int persistent_grid(int cls) {
   return sms * per_sm;
 }
 
-cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int cls) {
-  if (cls == BATCH_CUBE_TRI) render_batch_kernel<BATCH_CUBE_TRI><<<grid, kThreads, 0, s>>>(b);
-  else if (cls == BATCH_CUBE_TRI_COMPACT) render_batch_kernel<BATCH_CUBE_TRI_COMPACT><<<grid, kThreads, 0, s>>>(b);
-  else if (cls == BATCH_CMEM) render_batch_kernel<BATCH_CMEM><<<grid, kThreads, 0, s>>>(b);
-  else if (cls == BATCH_CUBE_NEAREST) render_batch_kernel<BATCH_CUBE_NEAREST><<<grid, kThreads, 0, s>>>(b);
-  else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b);
+cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int cls, const CmemParam* model) {
+  CmemParam cp{};
+  if (model) cp = *model;
+  if (cls == BATCH_CUBE_TRI) render_batch_kernel<BATCH_CUBE_TRI><<<grid, kThreads, 0, s>>>(b, cp);
+  else if (cls == BATCH_CUBE_TRI_COMPACT) render_batch_kernel<BATCH_CUBE_TRI_COMPACT><<<grid, kThreads, 0, s>>>(b, cp);
+  else if (cls == BATCH_CMEM) render_batch_kernel<BATCH_CMEM><<<grid, kThreads, 0, s>>>(b, cp);
+  else if (cls == BATCH_CUBE_NEAREST) render_batch_kernel<BATCH_CUBE_NEAREST><<<grid, kThreads, 0, s>>>(b, cp);
+  else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b, cp);
   return cudaGetLastError();
+}
+
+const void* render_batch_function(int cls) {
+  if (cls == BATCH_CUBE_TRI) return (const void*)render_batch_kernel<BATCH_CUBE_TRI>;
+  if (cls == BATCH_CUBE_TRI_COMPACT) return (const void*)render_batch_kernel<BATCH_CUBE_TRI_COMPACT>;
+  if (cls == BATCH_CMEM) return (const void*)render_batch_kernel<BATCH_CMEM>;
+  if (cls == BATCH_CUBE_NEAREST) return (const void*)render_batch_kernel<BATCH_CUBE_NEAREST>;
+  return (const void*)render_batch_kernel<BATCH_ANY>;
 }
 
 bool read_bounds_status(unsigned long long* status, bool reset) {

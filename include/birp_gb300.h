@@ -311,6 +311,14 @@ birp_status birp_measure_peaks(double* fp32_tflops, double* l2_read_gbs, size_t*
  * self-check of the margin the kernels use; margin receives that margin). */
 birp_status birp_cmem_margin_check(const birp_cmem* cmem, int n, float* max_rel_err, float* margin);
 
+/* The CMEM kernel's fast functions evaluated on the GPU beside CUDA's own at
+ * the same n FP32 arguments (host arrays): which = 0 its atan2 for y >= 0
+ * (atan2_pos(y, x) vs atan2f(y, x)), 1 its power (pow_pos(x, y) vs powf), 2
+ * its square root (sqrt_fast(x) vs sqrtf), 3 its base-2 exponential (ex2_fast
+ * vs exp2f); y is ignored by 2 and 3. A self-check of the error bounds the
+ * CMEM kernel relies on; no counterpart in the reference. */
+birp_status birp_fastmath_check(int which, const float* x, const float* y, int n, float* fast, float* lib);
+
 #ifdef __cplusplus
 }
 #endif
