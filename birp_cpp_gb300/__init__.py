@@ -31,7 +31,8 @@ class Camera(C.Structure):
     _fields_ = [("pos", C.c_double * 3), ("aim", C.c_double * 3), ("fov_w_deg", C.c_double),
                 ("fov_h_deg", C.c_double), ("nx", C.c_int), ("ny", C.c_int), ("n_samples", C.c_int),
                 ("ray_length", C.c_double), ("trilinear", C.c_int), ("march", C.c_int),
-                ("segments", C.c_int), ("roll_deg", C.c_double)]
+                ("segments", C.c_int), ("roll_deg", C.c_double), ("warp_rays_x", C.c_int),
+                ("tile_warps_x", C.c_int)]
 
 
 class CmemParams(C.Structure):
@@ -155,7 +156,7 @@ def shutdown() -> None:
 
 
 def camera(pos, aim, fov_w, fov_h, nx, ny, n_samples=200, ray_length=44.0, trilinear=True, march=PREFIX,
-           segments=0, roll=0.0) -> Camera:
+           segments=0, roll=0.0, warp_rays_x=0, tile_warps_x=0) -> Camera:
     c = Camera()
     for i in range(3):
         c.pos[i] = float(pos[i])
@@ -164,6 +165,7 @@ def camera(pos, aim, fov_w, fov_h, nx, ny, n_samples=200, ray_length=44.0, trili
     c.n_samples, c.ray_length = int(n_samples), float(ray_length)
     c.trilinear, c.march, c.segments = int(bool(trilinear)), int(march), int(segments)
     c.roll_deg = float(roll)
+    c.warp_rays_x, c.tile_warps_x = int(warp_rays_x), int(tile_warps_x)
     return c
 
 

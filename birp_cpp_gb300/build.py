@@ -93,6 +93,24 @@ def build_debug_bounds() -> str:
     return DEBUG_LIB
 
 
+def build_variant(defines: dict, tag: str) -> str:
+    """lib/libbirp_gb300_<tag>.so: render.cu compiled with the given macro
+    definitions (the autotuner's candidates), the other units as built."""
+    build()
+    out = os.path.join(OBJ, f"render_{tag}.o")
+    src = os.path.join(CSRC, "render.cu")
+    cmd = [nvcc()] + _flags() + [f"-D{k}={v}" for k, v in defines.items()] + ["-c", src, "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    lib = os.path.join(LIBDIR, f"libbirp_gb300_{tag}.so")
+    objs = [out] + [os.path.join(OBJ, os.path.splitext(s)[0] + ".o") for s in SOURCES if s != "render.cu"]
+    r = subprocess.run([nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lpthread"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed\n{r.stdout}\n{r.stderr}")
+    return lib
+
+
 def build_cli() -> str:
     """The command-line front-end (cli/birp.cpp) over the classes: lib/birp."""
     src = os.path.join(HERE, "cli", "birp.cpp")

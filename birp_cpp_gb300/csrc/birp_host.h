@@ -97,7 +97,11 @@ birp_status ensure_xyz_scratch(size_t floats);
 // cmem_host.cpp
 void cmem_coefficients(const birp_cmem_params& p, CmemDev& m);
 
-// tune.cpp: lanes-per-ray choice from the committed tuning table
-int tuned_seg_log2(int64_t pixels, int n_samples, int kind, int trilinear, bool batched);
+// tune.cpp: tile shape from the committed tuning tables (-1: the default for
+// the lanes per ray)
+struct TunedShape {
+  int seg_log2, wbx_l2, wgx_l2;
+};
+TunedShape tuned_shape(int64_t pixels, int n_samples, int kind, int trilinear, bool batched);
 
 }  // namespace birp

@@ -130,6 +130,8 @@ struct RequestDev {
   int interp;        // 1 trilinear, 0 nearest
   int kind;          // SpaceKind
   int seg_log2;      // rays are split over 2^seg_log2 lanes
+  int wbx_l2;        // a warp marches 2^wbx_l2 rays across
+  int wgx_l2;        // 2^wgx_l2 of the CTA's 4 warps sit across the tile
   int tiles_x;       // tiles along x for this request's tile shape
   int tiles;         // total tiles
   int compact;       // cube: 1 in the compact layout (node values, no records)
@@ -206,7 +208,12 @@ cudaError_t launch_peak_fp32(float* sink, int blocks, int iters, cudaStream_t st
 cudaError_t launch_fastmath(int which, const float* x, const float* y, int n, float* fast, float* lib,
                             cudaStream_t stream);
 cudaError_t launch_peak_read(const float4* buf, size_t n4, int reps, float* sink, int blocks, cudaStream_t stream);
-int tile_w(int seg_log2);
-int tile_h(int seg_log2);
+// Pixel tile of a request's tile shape (lanes per ray 2^seg_log2, warp-block
+// width 2^wbx_l2 rays, 2^wgx_l2 warps across the tile), whether the kernels
+// take that shape, and the default warp-block width for seg_log2.
+int tile_w(int seg_log2, int wbx_l2, int wgx_l2);
+int tile_h(int seg_log2, int wbx_l2, int wgx_l2);
+bool tile_shape_ok(int seg_log2, int wbx_l2, int wgx_l2);
+int default_wbx_l2(int seg_log2);
 
 }  // namespace birp

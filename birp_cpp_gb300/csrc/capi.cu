@@ -180,17 +180,33 @@ birp_status validate_camera(const birp_camera* c) {
     return fail(BIRP_ERR_INVALID, "march must be PREFIX or CLIP");
   if (!(c->segments == 0 || c->segments == 1 || c->segments == 2 || c->segments == 4 || c->segments == 8))
     return fail(BIRP_ERR_INVALID, "segments must be 0, 1, 2, 4 or 8");
+  auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+  if (c->warp_rays_x < 0 || (c->warp_rays_x > 0 && !pow2(c->warp_rays_x)) || c->tile_warps_x < 0 ||
+      (c->tile_warps_x > 0 && !pow2(c->tile_warps_x)) || c->tile_warps_x > 4)
+    return fail(BIRP_ERR_INVALID, "warp_rays_x and tile_warps_x must be 0 or powers of two (tile_warps_x <= 4)");
   return BIRP_OK;
 }
 
-// Lanes per ray: explicit, else the tuned tables (tune.cpp).
-int choose_seg_log2(const birp_camera& c, int kind, bool batched) {
-  if (c.segments > 0) {
-    int l = 0;
-    while ((1 << l) < c.segments) ++l;
-    return l;
-  }
-  return tuned_seg_log2((int64_t)c.nx * c.ny, c.n_samples, kind, c.trilinear, batched);
+namespace {
+int log2_of(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+}  // namespace
+
+// Tile shape: lanes per ray, warp-block width and warps across a tile, each
+// explicit or else from the tuned tables (tune.cpp).
+birp_status choose_shape(const birp_camera& c, int kind, bool batched, int& seg, int& wbx, int& wgx) {
+  TunedShape t = tuned_shape((int64_t)c.nx * c.ny, c.n_samples, kind, c.trilinear, batched);
+  seg = c.segments > 0 ? log2_of(c.segments) : t.seg_log2;
+  wbx = c.warp_rays_x > 0 ? log2_of(c.warp_rays_x) : (t.wbx_l2 >= 0 && c.segments == 0 ? t.wbx_l2 : default_wbx_l2(seg));
+  wgx = c.tile_warps_x > 0 ? log2_of(c.tile_warps_x) : (t.wgx_l2 >= 0 && c.segments == 0 ? t.wgx_l2 : 1);
+  if (!tile_shape_ok(seg, wbx, wgx))
+    return fail(BIRP_ERR_INVALID, "tile shape (%d lanes per ray, %d rays across a warp block, %d warps across a tile) "
+                                  "is not one the kernels take (tiles up to 32 pixels a side)",
+                1 << seg, 1 << wbx, 1 << wgx);
+  return BIRP_OK;
 }
 
 birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const birp_camera& c, float* out,
@@ -224,9 +240,10 @@ birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const bi
   r.mode = c.march;
   r.interp = c.trilinear ? 1 : 0;
   r.kind = cube ? SPACE_CUBE : SPACE_CMEM;
-  r.seg_log2 = choose_seg_log2(c, r.kind, batched);
-  r.tiles_x = (c.nx + tile_w(r.seg_log2) - 1) / tile_w(r.seg_log2);
-  int tiles_y = (c.ny + tile_h(r.seg_log2) - 1) / tile_h(r.seg_log2);
+  if (birp_status s2 = choose_shape(c, r.kind, batched, r.seg_log2, r.wbx_l2, r.wgx_l2)) return s2;
+  const int tw = tile_w(r.seg_log2, r.wbx_l2, r.wgx_l2), th = tile_h(r.seg_log2, r.wbx_l2, r.wgx_l2);
+  r.tiles_x = (c.nx + tw - 1) / tw;
+  int tiles_y = (c.ny + th - 1) / th;
   r.tiles = r.tiles_x * tiles_y;
   r.out = out;
   if (cube) {

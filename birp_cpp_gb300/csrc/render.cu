@@ -34,17 +34,20 @@ namespace birp {
 namespace {
 
 constexpr int kThreads = 128;
+// Resident CTAs per SM each persistent batch kernel class is compiled for:
+// the autotuner's choice (tune_launch.inc) unless given at compile time.
+#include "tune_launch.inc"
 #ifndef BIRP_WALK_MINB
-#define BIRP_WALK_MINB 8  // resident CTAs per SM of the records-layout trilinear batch kernel
+#define BIRP_WALK_MINB BIRP_WALK_MINB_TUNED  // records-layout trilinear
 #endif
 #ifndef BIRP_COMPACT_MINB
-#define BIRP_COMPACT_MINB 7  // ... of the compact-layout trilinear batch kernel (forms 8 corners per cell)
+#define BIRP_COMPACT_MINB BIRP_COMPACT_MINB_TUNED  // compact-layout trilinear (forms 8 corners per cell)
 #endif
 #ifndef BIRP_NEAREST_MINB
-#define BIRP_NEAREST_MINB 8  // resident CTAs per SM of the nearest-mode batch kernel
+#define BIRP_NEAREST_MINB BIRP_NEAREST_MINB_TUNED  // nearest mode
 #endif
 #ifndef BIRP_CMEM_MINB
-#define BIRP_CMEM_MINB 6  // resident CTAs per SM the CMEM batch kernel is compiled for
+#define BIRP_CMEM_MINB BIRP_CMEM_MINB_TUNED  // CMEM
 #endif
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
@@ -67,20 +70,16 @@ constexpr float kDirErr = 8e-7f;
 
 // ---------------------------------------------------------------- tile shape
 
-// Warp block (rays) for S = 2^segl2 lanes per ray: 32/S rays.
-__host__ __device__ constexpr int wb_x(int segl2) {
-  return segl2 == 0 ? 8 : segl2 == 1 ? 4 : segl2 == 2 ? 4 : segl2 == 3 ? 2 : segl2 == 4 ? 2 : 1;
-}
-__host__ __device__ constexpr int wb_y(int segl2) {
-  return segl2 == 0 ? 4 : segl2 == 1 ? 4 : segl2 == 2 ? 2 : segl2 == 3 ? 2 : segl2 == 4 ? 1 : 1;
-}
-// CTA tile = 2 x 2 warp blocks.
-__host__ __device__ constexpr int tw_of(int segl2) { return 2 * wb_x(segl2); }
-__host__ __device__ constexpr int th_of(int segl2) { return 2 * wb_y(segl2); }
+// Tile shape of a request (RequestDev::seg_log2, wbx_l2, wgx_l2): a warp
+// marches a 2^wbx_l2 x (32 / S / 2^wbx_l2) block of rays (S = 2^seg_log2
+// lanes per ray), and the CTA's 4 warps sit 2^wgx_l2 x (4 / 2^wgx_l2) over
+// its pixel tile. Tiles are at most kMaxTile pixels on a side (the host
+// checks; tile_shape_ok).
+constexpr int kMaxTile = 32;
 
 struct TileSmem {
-  double A[16][3];  // per column: sx*R[:,0] - R[:,2]
-  double B[8][3];   // per row:    sy*R[:,1]
+  double A[kMaxTile][3];  // per column: sx*R[:,0] - R[:,2]
+  double B[kMaxTile][3];  // per row:    sy*R[:,1]
 };
 
 // ---------------------------------------------------------------- helpers
@@ -290,8 +289,9 @@ __device__ __forceinline__ float rsqrt_fast(float x) {
 // (Lawson's iteratively reweighted least squares in FP64, rounded once to
 // FP32; tests/fit_atan2.py regenerates these lines; largest error 9.8e-8 rad
 // evaluated in FP32); then atan(y/|x|) = pi/2 - atan(|x|/y) when y > |x|, and
-// pi - atan(y/|x|) when x < 0. Error <= ~3e-7 rad with the hardware-reciprocal
-// division (checked against atan2f on the GPU by tests/test_gpu_fastmath.py).
+// pi - atan(y/|x|) when x < 0. Error <= 4e-7 rad with the hardware-reciprocal
+// division and the FP32 pi/2 and pi (checked against the true values and
+// atan2f on the GPU by tests/test_gpu_fastmath.py).
 __device__ __forceinline__ float atan2_pos(float y, float x) {
   const float ax = fabsf(x);
   const float a = __fdividef(fminf(ax, y), fmaxf(ax, y));
@@ -618,8 +618,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
                                             KernelStats* stats, const CmemParam* P = nullptr) {
   const int SEGL2 = R.seg_log2;
   const int S = 1 << SEGL2;
-  const int WBX = wb_x(SEGL2), WBY = wb_y(SEGL2);
-  const int TW = 2 * WBX, TH = 2 * WBY;
+  const int WBXL2 = R.wbx_l2, WGXL2 = R.wgx_l2;
+  const int WBX = 1 << WBXL2, WBY = (32 >> SEGL2) >> WBXL2;  // rays of a warp block
+  const int WGX = 1 << WGXL2, WGY = 4 >> WGXL2;               // warps of the tile
+  const int TW = WGX * WBX, TH = WGY * WBY;
   const int tid = threadIdx.x;
   const int x0 = tx * TW, y0 = ty * TH;
   const int nx = R.nx, ny = R.ny;
@@ -641,8 +643,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 
   const int warp = tid >> 5, lane = tid & 31;
   const int seg = lane & (S - 1), rw = lane >> SEGL2;
-  const int lx = (warp & 1) * WBX + (rw % WBX);
-  const int ly = (warp >> 1) * WBY + (rw / WBX);
+  const int lx = ((warp & (WGX - 1)) << WBXL2) + (rw & (WBX - 1));
+  const int ly = (warp >> WGXL2) * WBY + (rw >> WBXL2);
   const int pi = x0 + lx, pj = y0 + ly;
   const bool valid = pi < nx && pj < ny;
 
@@ -1636,11 +1638,17 @@ cudaError_t launch_peak_read(const float4* buf, size_t n4, int reps, float* sink
   return cudaGetLastError();
 }
 
-int tile_w(int segl2) { return tw_of(segl2); }
-int tile_h(int segl2) { return th_of(segl2); }
+int tile_w(int segl2, int wbx_l2, int wgx_l2) { return (1 << wgx_l2) << wbx_l2; }
+int tile_h(int segl2, int wbx_l2, int wgx_l2) { return ((32 >> segl2) >> wbx_l2) * (4 >> wgx_l2); }
+bool tile_shape_ok(int segl2, int wbx_l2, int wgx_l2) {
+  return segl2 >= 0 && segl2 <= 5 && wbx_l2 >= 0 && (1 << wbx_l2) <= (32 >> segl2) && wgx_l2 >= 0 && wgx_l2 <= 2 &&
+         tile_w(segl2, wbx_l2, wgx_l2) <= kMaxTile && tile_h(segl2, wbx_l2, wgx_l2) <= kMaxTile;
+}
+int default_wbx_l2(int segl2) { return segl2 == 0 ? 3 : segl2 <= 2 ? 2 : segl2 <= 4 ? 1 : 0; }
 
 cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStream_t s, const CmemDev* cmem_host) {
-  dim3 grid((h.nx + tw_of(h.seg_log2) - 1) / tw_of(h.seg_log2), (h.ny + th_of(h.seg_log2) - 1) / th_of(h.seg_log2));
+  const int tw = tile_w(h.seg_log2, h.wbx_l2, h.wgx_l2), th = tile_h(h.seg_log2, h.wbx_l2, h.wgx_l2);
+  dim3 grid((h.nx + tw - 1) / tw, (h.ny + th - 1) / th);
   CmemParam cp{};
   if (h.kind == SPACE_CMEM && cmem_host) {
     cp.m = *cmem_host;

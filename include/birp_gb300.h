@@ -123,7 +123,12 @@ typedef enum { BIRP_MARCH_PREFIX = 0, BIRP_MARCH_CLIP = 1 } birp_march;
  * segments: lanes per ray (1, 2, 4, 8), 0 = tuned choice. roll_deg: a roll
  * about the view axis in degrees, added to the Sun-fixed roll angle of
  * Camera::Orient (src/Camera.cpp:309-417); 0 (the default) is the
- * reference's pose exactly (an extension: the reference has no roll input). */
+ * reference's pose exactly (an extension: the reference has no roll input).
+ * warp_rays_x, tile_warps_x: the kernels' tile shape, a power of two each
+ * (0 = tuned choice): rays across the block of rays one warp marches (of its
+ * 32 / segments), and warps across a pixel tile (of 4, so 1, 2 or 4); tiles
+ * are at most 32 pixels on a side. The image is the same for every shape
+ * (lanes per ray change only the order of the sum). */
 typedef struct {
   double pos[3];
   double aim[3];
@@ -135,6 +140,8 @@ typedef struct {
   int march;
   int segments;
   double roll_deg;
+  int warp_rays_x;
+  int tile_warps_x;
 } birp_camera;
 
 /* Fills the reference's CLI defaults (src/main.cpp:37-63): pos

@@ -192,3 +192,33 @@ def test_server_lru_eviction_and_errors(birp, spaces):
     for t in tickets:
         assert srv.wait(t, 60000).status == 0
     srv.close()
+
+
+def test_tile_shapes_give_the_same_images(birp, spaces):
+    """Every tile shape the kernels take (rays across a warp block, warps
+    across a tile) renders the same image, bit for bit, for a given number of
+    lanes per ray: the shape only maps rays to lanes. Plain and batched, cube
+    (both interpolations) and CMEM; shapes the kernels do not take are
+    rejected."""
+    from birp_cpp_gb300 import autotune
+    pos, aim = (-2.0, -12.0, 16.0), (9.0, 0.0, 0.0)
+    b = birp.Batch(64, 1 << 22)
+    for space, tri in ((spaces["c1"], True), (spaces["c1"], False), (spaces["cmem"], True)):
+        for seg in (1, 2, 8):
+            ref = None
+            items = []
+            for wx, gx in autotune.shapes(seg):
+                cam = birp.camera(pos, aim, 27.0, 16.0, 37, 23, n_samples=300, segments=seg, warp_rays_x=wx,
+                                  tile_warps_x=gx, trilinear=tri)
+                img = birp.render(space, cam)
+                if ref is None:
+                    ref = img
+                assert np.array_equal(img, ref), (seg, wx, gx)
+                items.append((space, cam))
+            for img in b.render(items):
+                assert np.array_equal(img, ref)
+    b.close()
+    for wx, gx, seg in ((3, 2, 1), (64, 1, 1), (32, 2, 1), (8, 8, 1), (16, 1, 8)):
+        cam = birp.camera(pos, aim, 27.0, 16.0, 37, 23, n_samples=300, segments=seg, warp_rays_x=wx, tile_warps_x=gx)
+        with pytest.raises(birp.BirpError):
+            birp.render(spaces["c1"], cam)

@@ -4,8 +4,9 @@ sqrtf / exp2f at the same FP32 arguments, on dense grids over the argument
 ranges the CMEM model gives them. The bounds asserted are the ones the
 kernel's FP32 shell decisions are budgeted with (its margin is checked
 separately by birp_cmem_margin_check):
-  atan2_pos   <= 3e-7 rad absolute (degree-8 minimax polynomial, 9.8e-8 rad,
-              plus the hardware-reciprocal division of min/max)
+  atan2_pos   <= 4e-7 rad absolute (degree-8 minimax polynomial, 9.8e-8 rad;
+              the hardware-reciprocal division of min/max; the FP32 pi/2
+              and pi it is subtracted from and that last rounding)
   sqrt_fast   <= 3 ulp relative (x * rsqrt.approx)
   ex2_fast    <= 2 ulp relative (ex2.approx.ftz)
   pow_pos     relative error <= 5e-7 + 2.5e-7 |y log2 x| (ex2.approx of
@@ -38,9 +39,9 @@ def test_atan2_pos(birp):
     fast, lib = birp.fastmath_check(0, x, y)
     true = np.arctan2(y.astype(np.float64), x.astype(np.float64))
     err = np.abs(fast - true)
-    assert err.max() <= 3e-7, (err.max(), x[err.argmax()], y[err.argmax()])
-    assert np.abs(fast.astype(np.float64) - lib).max() <= 3.5e-7
-    assert fast.min() >= 0.0 and fast.max() <= np.float32(np.pi) + 3e-7
+    assert err.max() <= 4e-7, (err.max(), x[err.argmax()], y[err.argmax()])
+    assert np.abs(fast.astype(np.float64) - lib).max() <= 4.5e-7
+    assert fast.min() >= 0.0 and fast.max() <= np.float32(np.pi) + 4e-7
 
 
 def test_sqrt_fast(birp):
