@@ -99,9 +99,9 @@ def tune_plain(n_poses: int = 4, repeats: int = 3):
                     times[(s, wx, gx)] = tot / len(poses)
             best = min(times, key=times.get)
             results[(nx * ny, n)] = (best, times)
+            default = (best[0], 1 << [3, 2, 2, 1][SEGMENTS.index(best[0])], 2)  # the untuned shape of that S
             print(json.dumps({"context": "plain", "pixels": nx * ny, "n_samples": n, "best": best,
-                              "ms_best": round(times[best], 4),
-                              "ms_default_S": round(min(v for k, v in times.items() if k[0] == best[0]), 4)}),
+                              "ms_best": round(times[best], 4), "ms_default_shape": round(times[default], 4)}),
                   flush=True)
     return results
 

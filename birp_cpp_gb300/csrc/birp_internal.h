@@ -6,7 +6,8 @@
 //    + c7 xyz in the cell's local coordinates (x, y, z) = p - (lower node)
 //    (physical units, so a ray's step along an axis is the same in every
 //    cell), computed in FP64 from the FP32 corner values and stored FP32 as
-//    {c0, c1, c2, c4 | c3, c5, c6, c7}; c0 is the value of the cell's lower
+//    {c0, c3, c1, c5 | c2, c6, c4, c7} (the pairs the march's packed FP32x2
+//    FMAs take: {c0, c3}, {c1, c5}, {c2, c6}, {c4, c7}); c0 is the value of the cell's lower
 //    corner (node k). Records are x fastest for cells -1..n-1 on every axis:
 //    one guard cell each side whose outside corners repeat the edge node and
 //    whose coefficients along that axis are exactly 0, so a cell index that
@@ -192,6 +193,9 @@ cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t stream
 const void* render_batch_function(int cls);
 int persistent_grid(int cls);
 cudaError_t launch_cube_fill(const float* src_xfast, int nx, int ny, int nz, float* dst, cudaStream_t stream);
+// node values (x fastest; device memory or pinned host memory the device
+// reads) into the interior of the padded grid
+cudaError_t launch_cube_pad_copy(const float* src, int nx, int ny, int nz, float* dst, cudaStream_t stream);
 cudaError_t launch_cube_negflags(const float* padded, int nx, int ny, int nz, uint8_t* flags, cudaStream_t stream);
 // bounds-checking build: the first out-of-range access (code << 48 | index),
 // 0 if none, optionally reset; other builds: always 0, returns false

@@ -213,15 +213,24 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
                    (compact ? total * sizeof(float) + walk.size() * sizeof(float4)
                             : records * 2 * sizeof(float4) + walk2.size() * sizeof(float2));
 
-  // interior values: one strided 3D copy from the caller's x-fastest array
-  cudaMemcpy3DParms p;
-  std::memset(&p, 0, sizeof p);
-  p.srcPtr = make_cudaPitchedPtr((void*)values, (size_t)nx * sizeof(float), nx, ny);
-  p.dstPtr = make_cudaPitchedPtr(scalar, px * sizeof(float), px, py);
-  p.dstPos = make_cudaPos(sizeof(float), 1, 1);
-  p.extent = make_cudaExtent((size_t)nx * sizeof(float), ny, nz);
-  p.kind = cudaMemcpyHostToDevice;
-  CKU(cudaMemcpy3DAsync(&p, st));
+  // interior values from the caller's x-fastest array: pinned host memory
+  // (the server's copies) is read by a kernel straight into the padded grid;
+  // other (pageable) memory goes by one strided 3D copy
+  cudaPointerAttributes pa{};
+  const bool pinned = cudaPointerGetAttributes(&pa, values) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+  cudaGetLastError();  // (an unregistered pointer is not an error to keep)
+  if (pinned) {
+    CKU(launch_cube_pad_copy(values, nx, ny, nz, scalar, st));
+  } else {
+    cudaMemcpy3DParms p;
+    std::memset(&p, 0, sizeof p);
+    p.srcPtr = make_cudaPitchedPtr((void*)values, (size_t)nx * sizeof(float), nx, ny);
+    p.dstPtr = make_cudaPitchedPtr(scalar, px * sizeof(float), px, py);
+    p.dstPos = make_cudaPos(sizeof(float), 1, 1);
+    p.extent = make_cudaExtent((size_t)nx * sizeof(float), ny, nz);
+    p.kind = cudaMemcpyHostToDevice;
+    CKU(cudaMemcpy3DAsync(&p, st));
+  }
   CKU(launch_cube_fill(nullptr, nx, ny, nz, scalar, st));
   if (c.has_neg) CKU(launch_cube_negflags(scalar, nx, ny, nz, c.d_negflag, st));
   // (the host vectors below stay alive until the synchronize at the end)

@@ -347,7 +347,11 @@ __device__ __forceinline__ float pow_pos(float a, float b) { return ex2_fast(b *
 
 constexpr float kLog2e = 1.4426950408889634f;
 
-__device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d, float& r_mp, float& r_bs) {
+// r_mp and r_bs in FP32; mp_terms = |p0 r0 f| + |q|, the size of the two
+// terms whose sum is r_mp (near the cusps q cancels most of the first, and
+// r_mp's absolute FP32 error follows mp_terms, not r_mp).
+__device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d, float& r_mp, float& r_bs,
+                                             float& mp_terms) {
   // angle to the northern / southern cusp axes
   const float ux = d.ct, uy = d.st * d.cp, uz = d.st * d.sp;
   float dn = ux * m.cos_tn + uz * m.sin_tn;
@@ -362,6 +366,7 @@ __device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d,
   float q = m.p2c * ex2_fast(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
             m.p2c * ex2_fast(kLog2e * m.p3ds * pow_pos(phi_s, m.a21));
   r_mp = m.p0r0 * f + q;
+  mp_terms = fabsf(m.p0r0 * f) + fabsf(q);
   const float lb = __log2f(d.b2);
   float ry = m.bs * ex2_fast(m.ay * lb);
   float rz = m.bs * ex2_fast(m.az * lb);
@@ -371,8 +376,8 @@ __device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d,
 
 __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
   const CmemDir d = cmem_dir32(x, y, z);
-  float r_mp, r_bs;
-  cmem_radii32(m, d, r_mp, r_bs);
+  float r_mp, r_bs, mp_terms;
+  cmem_radii32(m, d, r_mp, r_bs, mp_terms);
   const float r = d.r;
   const float half = 0.025f;
   CmemEval out;
@@ -396,6 +401,14 @@ __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, floa
     const float d10 = r * 0.1f;
     outer = __fdividef(m.A2, d10 * d10 * d10);
   }
+  // The magnetopause ramp's value is sheath * (r - r_mp + 1/2 thickness) /
+  // (r_mp + 1/2 thickness): its FP32 error is about sheath * (error of r -
+  // r_mp) / (r_mp + 1/2 thickness), and r_mp's error follows the size of its
+  // terms (mp_terms). Where the cusp term cancels most of r_mp (r_mp well
+  // under its terms, down to a fraction of an Earth radius near the Earth),
+  // that error is a large part of the sheath value, which there is large:
+  // such samples take the FP64 path.
+  if (shell == 1 && !(mp_terms + r <= 4.f * (r_mp + half))) out.unsure = true;
   float v;
   if (shell == 0) v = 0.f;
   else if (shell == 1) v = lerp_f(0.f, sheath, (r - (r_mp - half)) / (r_mp + half));
@@ -925,7 +938,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
       int ncell = 0;
       int guard = 0;
       while (u < ub) {
-        float4 lo, hi;  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
+        float4 lo, hi;  // {c0, c3, c1, c5}, {c2, c6, c4, c7}
         if constexpr (COMPACT) {
           // the cell's trilinear coefficients from its 8 corners, in local
           // physical coordinates (scaled by the inverse widths)
@@ -940,8 +953,8 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           const float e4 = t - d1, e5 = w - d1, e6 = (v110 - v100) - d2;
           const float e7 = ((v111 - v110) - w) - e4;
           const float ixy = iw[0] * iw[1];
-          lo = make_float4(v000, d1 * iw[0], d2 * iw[1], e4 * ixy);
-          hi = make_float4(d3 * iw[2], e5 * (iw[0] * iw[2]), e6 * (iw[1] * iw[2]), e7 * (ixy * iw[2]));
+          lo = make_float4(v000, d3 * iw[2], d1 * iw[0], e5 * (iw[0] * iw[2]));
+          hi = make_float4(d2 * iw[1], e6 * (iw[1] * iw[2]), e4 * ixy, e7 * (ixy * iw[2]));
         } else {
 #ifdef BIRP_DEBUG_BOUNDS
           if (!bound_ok(q - C.rec, C.rec_f4 - 1, 6)) q = C.rec;
@@ -952,17 +965,22 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         const float nxt = fminf(ceilf(fminf(fminf(ex[0], ex[1]), ex[2])), ub);
         if (nxt > u) {
           const float m = nxt - u;
-          const float X = fmaf(u, st[0], xb[0]), Y = fmaf(u, st[1], xb[1]), Z = fmaf(u, st[2], xb[2]);
-          // value, gradient and mixed second derivatives at the first sample
-          const float b0 = fmaf(lo.y, X, lo.x);  // c0 + c1 X
-          const float a0 = fmaf(lo.w, X, lo.z);  // c2 + c4 X
-          const float b1 = fmaf(hi.y, X, hi.x);  // c3 + c5 X
-          const float a1 = fmaf(hi.w, X, hi.z);  // c6 + c7 X  (= f_yz)
-          const float lowz = fmaf(a0, Y, b0), gz = fmaf(a1, Y, b1);
+          // pairs of independent FMAs as one packed FP32x2 instruction (the
+          // record's float4 halves are the pairs: {c0, c3}, {c1, c5}, {c2,
+          // c6}, {c4, c7}); the same roundings as two scalar FMAs
+          const float2 XY = __ffma2_rn(make_float2(u, u), make_float2(st[0], st[1]), make_float2(xb[0], xb[1]));
+          const float X = XY.x, Y = XY.y, Z = fmaf(u, st[2], xb[2]);
+          // value, gradient and mixed second derivatives at the first sample:
+          // (c0 + c1 X, c3 + c5 X), (c2 + c4 X, c6 + c7 X), then
+          // (c0 + c1 X + (c2 + c4 X) Y, c3 + c5 X + (c6 + c7 X) Y) = (f at z = 0, f_z)
+          const float2 Bv = __ffma2_rn(make_float2(lo.z, lo.w), make_float2(X, X), make_float2(lo.x, lo.y));
+          const float2 Av = __ffma2_rn(make_float2(hi.z, hi.w), make_float2(X, X), make_float2(hi.x, hi.y));
+          const float2 LG = __ffma2_rn(Av, make_float2(Y, Y), Bv);
+          const float a0 = Av.x, a1 = Av.y, lowz = LG.x, gz = LG.y;
           const float f0v = fmaf(gz, Z, lowz);
           const float gy = fmaf(a1, Z, a0);
-          const float hxy = fmaf(hi.w, Z, lo.w), hxz = fmaf(hi.w, Y, hi.y);  // c4 + c7 Z, c5 + c7 Y
-          const float gx = fmaf(hxz, Z, fmaf(lo.w, Y, lo.y));  // c1 + c4 Y + c5 Z + c7 Y Z
+          const float hxy = fmaf(hi.w, Z, hi.z), hxz = fmaf(hi.w, Y, lo.w);  // c4 + c7 Z, c5 + c7 Y
+          const float gx = fmaf(hxz, Z, fmaf(hi.z, Y, lo.z));  // c1 + c4 Y + c5 Z + c7 Y Z
           const float p1 = fmaf(gx, st[0], fmaf(gy, st[1], gz * st[2]));
           const float p2 = fmaf(hxy, DxDy, fmaf(hxz, DxDz, a1 * DyDz));
           const float p3 = hi.w * DxDyDz;
@@ -1243,21 +1261,34 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     }
     n_exact_nearest = n_fp64;
   } else {
-    float st[3], bs[3];
+    // Sample positions p + d ((i + 1/2) dt) from the ray's FP64 direction:
+    // the step d dt and the first position as float pairs (hi + lo), so a
+    // position is fma(i, st_hi, bs_hi) + fma(i, st_lo, bs_lo), within about
+    // one FP32 ulp of the FP64 position at any distance along the ray (an
+    // FP32 direction would put a sample t * 1e-7 Re off, a large relative
+    // error near the Earth, where the model's values are largest).
+    need_d64();
+    float st[3], bs[3], st_lo[3], bs_lo[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      st[k] = R.dt32 * d32[k];
-      bs[k] = fmaf(0.5f, st[k], R.pos32[k]);
+      const double s64 = __dmul_rn(d64[k], R.dt), b64 = __dadd_rn(R.pos[k], __dmul_rn(0.5, s64));
+      st[k] = (float)s64;
+      st_lo[k] = (float)(s64 - (double)st[k]);
+      bs[k] = (float)b64;
+      bs_lo[k] = (float)(b64 - (double)bs[k]);
     }
-    // bound on |x32 - x64| of a sample, linear in the sample index
-    const float apos = fabsf(R.pos32[0]) + fabsf(R.pos32[1]) + fabsf(R.pos32[2]);
-    const float perr_slope = R.dt32 * (kDirErr + 5e-7f);
-    const float perr_base = 0.5f * perr_slope + apos * 5e-7f + 1e-6f;
+    // bound on |x32 - x64| of a sample: two FP32 roundings of a coordinate
+    // (the reach of the ray bounds every coordinate) and the float pairs'
+    // own error
+    const float reach = fabsf(R.pos32[0]) + fabsf(R.pos32[1]) + fabsf(R.pos32[2]) + 1.8f * (float)N * R.dt32;
+    const float perr = fmaf(1.2e-7f, reach, 1e-9f);
     auto march = [&](const CmemDev& M) {
 #pragma unroll 1
       for (int it = 0; it < iters; ++it) {
-        float x = fmaf(fi, st[0], bs[0]), y = fmaf(fi, st[1], bs[1]), z = fmaf(fi, st[2], bs[2]);
-        CmemEval e = cmem_value32(M, x, y, z, fmaf(fi, perr_slope, perr_base));
+        float x = fmaf(fi, st[0], bs[0]) + fmaf(fi, st_lo[0], bs_lo[0]);
+        float y = fmaf(fi, st[1], bs[1]) + fmaf(fi, st_lo[1], bs_lo[1]);
+        float z = fmaf(fi, st[2], bs[2]) + fmaf(fi, st_lo[2], bs_lo[2]);
+        CmemEval e = cmem_value32(M, x, y, z, perr);
         float v = e.v;
         if (e.unsure) {
           need_d64();
@@ -1407,6 +1438,19 @@ __global__ void cube_guard_kernel(float* dst, int nx, int ny, int nz) {
   }
 }
 
+// Copies the x-fastest node values into the interior of the padded grid
+// (node (i, j, k) to padded (i+1, j+1, k+1)), reading the source where it
+// lies: pinned host memory is read by the kernel itself (over NVLink-C2C on a
+// Grace host), one coalesced pass, instead of a strided 3D copy.
+__global__ void cube_pad_copy_kernel(const float* __restrict__ src, int nx, int ny, int nz, float* __restrict__ dst) {
+  const long long n = (long long)nx * ny * nz, px = nx + 2, pxy = (long long)(nx + 2) * (ny + 2);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const long long row = t / nx, x = t - row * nx;
+    const long long y = row % ny, z = row / ny;
+    dst[(z + 1) * pxy + (y + 1) * px + (x + 1)] = __ldcs(src + t);
+  }
+}
+
 // Cell records from the padded scalar grid ((nx+2)(ny+2)(nz+2), node i at
 // padded index i+1): record (a, b, c), a in [0, nx], is the trilinear
 // polynomial of the 8 padded nodes (a..a+1, b..b+1, c..c+1) (cell a-1 of the
@@ -1433,8 +1477,8 @@ __global__ void cube_records_kernel(const float* __restrict__ v, int nx, int ny,
     const double c5 = ((v101 - v100) - (v001 - v000)) * (ix * iz);
     const double c6 = ((v110 - v100) - (v010 - v000)) * (iy * iz);
     const double c7 = (((v111 - v110) - (v101 - v100)) - ((v011 - v010) - (v001 - v000))) * (ix * iy * iz);
-    rec[2 * r] = make_float4((float)v000, (float)c1, (float)c2, (float)c4);
-    rec[2 * r + 1] = make_float4((float)c3, (float)c5, (float)c6, (float)c7);
+    rec[2 * r] = make_float4((float)v000, (float)c3, (float)c1, (float)c5);
+    rec[2 * r + 1] = make_float4((float)c2, (float)c6, (float)c4, (float)c7);
   }
 }
 
@@ -1501,14 +1545,14 @@ __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int triline
       continue;
     }
     const float4* b = C.rec + 2 * record_index(C.cx, C.cxy, k[0], k[1], k[2]);
-    const float4 lo = b[0], hi = b[1];  // {c0, c1, c2, c4}, {c3, c5, c6, c7}
+    const float4 lo = b[0], hi = b[1];  // {c0, c3, c1, c5}, {c2, c6, c4, c7}
     if (!trilinear) {
       out[t] = lo.x;
       continue;
     }
     const double x = f[0], y = f[1], z = f[2];
-    const double bot = (double)lo.x + x * lo.y + y * ((double)lo.z + x * lo.w);
-    const double top = (double)hi.x + x * hi.y + y * ((double)hi.z + x * hi.w);
+    const double bot = (double)lo.x + x * lo.z + y * ((double)hi.x + x * hi.z);
+    const double top = (double)lo.y + x * lo.w + y * ((double)hi.y + x * hi.w);
     out[t] = (float)(bot + z * top);
   }
 }
@@ -1543,8 +1587,8 @@ __global__ void cmem_radii_check_kernel(const CmemDev* __restrict__ cmem, int n,
     const double ph0 = ((h >> 24) & 0xFFFFFF) * (pi / 16777216.0);
     const float x = (float)(10.0 * cos(th0)), y = (float)(10.0 * sin(th0) * cos(ph0)),
                 z = (float)(10.0 * sin(th0) * sin(ph0));
-    float r_mp, r_bs;
-    cmem_radii32(m, cmem_dir32(x, y, z), r_mp, r_bs);
+    float r_mp, r_bs, mp_terms;
+    cmem_radii32(m, cmem_dir32(x, y, z), r_mp, r_bs, mp_terms);
     const double X = x, Y = y, Z = z, R = sqrt(X * X + Y * Y + Z * Z);
     double th = (X != 0) ? acos(X / R) : 0.0, ph = (Y != 0) ? acos(Y / sqrt(Y * Y + Z * Z)) : 0.0;
     double phi_n = acos(cos(th) * cos(m.d_tn) + sin(th) * sin(m.d_tn) * cos(ph - pi / 2));
@@ -1713,6 +1757,16 @@ bool read_bounds_status(unsigned long long* status, bool reset) {
   (void)reset;
   return false;
 #endif
+}
+
+cudaError_t launch_cube_pad_copy(const float* src, int nx, int ny, int nz, float* dst, cudaStream_t s) {
+  const long long n = (long long)nx * ny * nz;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int blocks = (int)std::min<long long>((n + 255) / 256, (long long)std::max(sms, 1) * 8);
+  cube_pad_copy_kernel<<<blocks, 256, 0, s>>>(src, nx, ny, nz, dst);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_cube_fill(const float*, int nx, int ny, int nz, float* dst, cudaStream_t s) {

@@ -114,3 +114,33 @@ def test_server_compact_cubes(birp, cubes):
     st = srv.stats()
     assert 0 < st.resident_bytes < 1.1 * 130 ** 3 * 4 + (1 << 20)
     srv.close()
+
+
+def test_pinned_values_upload_equals_pageable(birp):
+    """Cube values in pinned host memory (as the server keeps them) are read
+    by a kernel straight into the device layout; pageable values go by a 3D
+    copy. Both give the same cube: renders equal bit for bit, both layouts."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    from birp_cpp_gb300 import synth
+    xs, ys, zs, v = synth.cube_config1(seed=5, n=72)
+    v32 = v.astype(np.float32)
+    pinned = torch.from_numpy(v32.copy()).pin_memory()
+    assert pinned.is_pinned()
+    cam = birp.camera((-2.0, -12.0, 16.0), (9.0, 0.0, 0.0), 27.0, 16.0, 96, 56, n_samples=880)
+    for layout in (birp.CUBE_RECORDS, birp.CUBE_COMPACT):
+        ref = birp.Cube(xs, ys, zs, v32, layout=layout)
+        h = C.c_void_p()
+        ax = [np.ascontiguousarray(a, np.float64) for a in (xs, ys, zs)]
+        birp.check(birp.lib().birp_cube_create_layout(ax[0].ctypes.data, len(xs), ax[1].ctypes.data, len(ys),
+                                                      ax[2].ctypes.data, len(zs), C.c_void_p(pinned.data_ptr()),
+                                                      int(layout), C.byref(h)))
+        try:
+            for tri in (True, False):
+                cam.trilinear = int(tri)
+                img = np.empty((cam.ny, cam.nx), np.float32)
+                birp.check(birp.lib().birp_render(h, None, C.byref(cam), img.ctypes.data, None))
+                assert np.array_equal(img, birp.render(ref, cam)), (layout, tri)
+        finally:
+            birp.lib().birp_cube_destroy(h)
+            ref.close()

@@ -9,9 +9,10 @@ separately by birp_cmem_margin_check):
               and pi it is subtracted from and that last rounding)
   sqrt_fast   <= 3 ulp relative (x * rsqrt.approx)
   ex2_fast    <= 2 ulp relative (ex2.approx.ftz)
-  pow_pos     relative error <= 5e-7 + 2.5e-7 |y log2 x| (ex2.approx of
-              y * log2.approx(x): the log's error grows with the result's
-              exponent)"""
+  pow_pos     relative error <= 5e-7 + 2.5e-7 |y log2 x| + 1.7e-7 |y|
+              (ex2.approx of y * log2.approx(x): the log's relative error
+              grows with the result's exponent, and near x = 1 its absolute
+              error, about 2^-22.5, is scaled by y)"""
 import numpy as np
 import pytest
 
@@ -70,7 +71,7 @@ def test_pow_pos(birp):
     x, y = _grid2(a, b)
     fast, lib = birp.fastmath_check(1, x, y)
     true = np.power(x.astype(np.float64), y.astype(np.float64))
-    bound = 5e-7 + 2.5e-7 * np.abs(y * np.log2(x.astype(np.float64)))
+    bound = 5e-7 + 2.5e-7 * np.abs(y * np.log2(x.astype(np.float64))) + 1.7e-7 * np.abs(y)
     rel = np.abs(fast - true) / true
     worst = int(np.argmax(rel / bound))
     assert np.all(rel <= bound), (rel[worst], bound[worst], x[worst], y[worst])
