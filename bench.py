@@ -591,7 +591,11 @@ def cpu_sample(reqs, host, seconds: float, threads: int, seed: int = 7):
 
 
 def run_reference(args, world, rank):
-    """--impl reference: the reference's CPU render arithmetic (oracle port)."""
+    """--impl reference: the reference's CPU render arithmetic (oracle port).
+    A step is a bounded sample: --ref-seconds of random pixels of the
+    workload on all host threads; ms_per_step is that step's measured time,
+    images_per_step the images its pixels amount to (pixels / the workload's
+    mean pixels per image), and value their ratio, images/s."""
     if rank != 0:
         return
     from birp_cpp_gb300 import synth
@@ -601,16 +605,20 @@ def run_reference(args, world, rank):
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_sample(reqs, host, 0.5, threads, seed=100)
-    vals, pxs, t_tot = [], 0, 0.0
+    vals, pxs, t_tot, walls = [], 0, 0.0, []
     for k in range(args.steps):
+        t0 = time.perf_counter()
         v, px, t = cpu_sample(reqs, host, args.ref_seconds, threads, seed=200 + k)
+        walls.append(time.perf_counter() - t0)
         vals.append(v)
         pxs += px
         t_tot += t
     value = float(np.mean(vals))
+    mean_px = float(np.mean([nx * ny for _, _, nx, ny, _ in reqs]))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * args.requests / value,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(walls)),
+        "images_per_step": pxs / args.steps / mean_px,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": config_dict(args),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
