@@ -136,6 +136,7 @@ struct RequestDev {
   int tiles_x;       // tiles along x for this request's tile shape
   int tiles;         // total tiles
   int compact;       // cube: 1 in the compact layout (node values, no records)
+  int has_neg;       // cube: 1 when it holds a value below zero (it carries flags)
   const CubeDev* cube;   // device pointer (kind == SPACE_CUBE)
   const CmemDev* cmem;   // device pointer (kind == SPACE_CMEM)
   float* out;            // ny*nx floats, row 0 = top
@@ -170,19 +171,21 @@ struct BatchDev {
 // kernel as a parameter
 cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaStream_t stream,
                                 const CmemDev* cmem_host = nullptr);
-// Persistent batch kernel classes: CUBE_TRI renders only trilinear cube
-// requests (fewer registers, more resident warps); ANY renders every kind.
-// Persistent-kernel classes: trilinear cube requests in the records layout,
-// the same in the compact layout, CMEM requests, nearest-mode cube requests
-// (either layout), and the general kernel that renders any request (used
-// where one launch must take a mix, see birp_batch_render_noalloc).
+// Persistent-kernel classes: trilinear cube requests in the records layout
+// (fewer registers, more resident warps than the general kernel), the same in
+// the compact layout, CMEM requests, nearest-mode cube requests (either
+// layout), trilinear requests of cubes holding a negative value (either
+// layout; FP64 sums next to negative nodes), and the general kernel that
+// renders any request (used where one launch must take a mix, see
+// birp_batch_render_noalloc).
 enum BatchClass : int {
   BATCH_CUBE_TRI = 0,
   BATCH_ANY = 1,
   BATCH_CUBE_TRI_COMPACT = 2,
   BATCH_CMEM = 3,
   BATCH_CUBE_NEAREST = 4,
-  BATCH_CLASSES = 5
+  BATCH_CUBE_SIGNED = 5,  // trilinear cubes holding a negative value, either layout
+  BATCH_CLASSES = 6
 };
 // model: the CMEM model the CMEM class kernel takes as a parameter (nullptr:
 // none, every request reads its model through its pointer)

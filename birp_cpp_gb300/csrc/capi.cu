@@ -249,6 +249,7 @@ birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const bi
   if (cube) {
     r.cube = cube->d_desc;
     r.compact = cube->h_desc.compact;
+    r.has_neg = cube->has_neg > 0 ? 1 : 0;
   } else {
     r.cmem = cmem->d_desc;
   }

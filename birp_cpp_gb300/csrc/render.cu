@@ -49,6 +49,9 @@ constexpr int kThreads = 128;
 #ifndef BIRP_CMEM_MINB
 #define BIRP_CMEM_MINB BIRP_CMEM_MINB_TUNED  // CMEM
 #endif
+#ifndef BIRP_SIGNED_MINB
+#define BIRP_SIGNED_MINB 4  // trilinear cubes holding negative values (either layout, FP64 cell sums)
+#endif
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
@@ -540,22 +543,20 @@ __device__ __forceinline__ double node_value(const CubeDev& C, int i, int j, int
 // column/row terms a + b): the exact cell of each coordinate (g: the FP32
 // guesses), FP64 fractions and lerps x -> y -> z, or the lower node's value
 // for nearest. Not inlined: it runs only for samples in flagged cells.
-__device__ __noinline__ bool sample_negative64(const CubeDev* Cp, int trilinear, const double* a, const double* b,
-                                               double px, double py, double pz, double dt, int i, int g0, int g1,
-                                               int g2) {
-  const CubeDev& C = *Cp;
-  double w[3], d[3];
-  for (int r = 0; r < 3; ++r) w[r] = __dadd_rn(a[r], b[r]);
-  dir64(w, d);
-  const double P[3] = {px, py, pz};
-  const int g[3] = {g0, g1, g2};
+// The FP64 oracle's value of in-box sample i of a ray (cube64_sample at
+// pos64 = P + d ((i + 1/2) dt), d the ray's FP64 direction): the exact cell of
+// each coordinate (g: guesses, updated to the cells found), FP64 fractions and
+// lerps x -> y -> z, or the lower node's value for nearest.
+__device__ __forceinline__ double sample_value64(const CubeDev& C, int trilinear, const double* d, const double* P,
+                                                 double dt, int i, int* g) {
   double p[3], f[3];
   int k[3];
   for (int r = 0; r < 3; ++r) {
     p[r] = pos64(P[r], d[r], dt, i);
     k[r] = exact_cell(C.ax[r], p[r], g[r]);
+    g[r] = k[r];
   }
-  if (!trilinear) return node_value(C, k[0], k[1], k[2]) < 0.0;
+  if (!trilinear) return node_value(C, k[0], k[1], k[2]);
   for (int r = 0; r < 3; ++r) {
     const double* c = C.ax[r].c64;
     f[r] = __ddiv_rn(__dsub_rn(p[r], c[k[r]]), __dsub_rn(c[k[r] + 1], c[k[r]]));
@@ -563,7 +564,38 @@ __device__ __noinline__ bool sample_negative64(const CubeDev* Cp, int trilinear,
   auto v = [&](int di, int dj, int dk) { return node_value(C, k[0] + di, k[1] + dj, k[2] + dk); };
   const double lx1 = lerp64(v(0, 0, 0), v(1, 0, 0), f[0]), lx2 = lerp64(v(0, 1, 0), v(1, 1, 0), f[0]);
   const double hx1 = lerp64(v(0, 0, 1), v(1, 0, 1), f[0]), hx2 = lerp64(v(0, 1, 1), v(1, 1, 1), f[0]);
-  return lerp64(lerp64(lx1, lx2, f[1]), lerp64(hx1, hx2, f[1]), f[2]) < 0.0;
+  return lerp64(lerp64(lx1, lx2, f[1]), lerp64(hx1, hx2, f[1]), f[2]);
+}
+
+__device__ __noinline__ bool sample_negative64(const CubeDev* Cp, int trilinear, const double* a, const double* b,
+                                               double px, double py, double pz, double dt, int i, int g0, int g1,
+                                               int g2) {
+  double w[3], d[3];
+  for (int r = 0; r < 3; ++r) w[r] = __dadd_rn(a[r], b[r]);
+  dir64(w, d);
+  const double P[3] = {px, py, pz};
+  int g[3] = {g0, g1, g2};
+  return sample_value64(*Cp, trilinear, d, P, dt, i, g) < 0.0;
+}
+
+// Sum, in FP64, of the FP64 oracle's values of the trilinear samples
+// [i0, i1) of a ray (its FP64 direction rebuilt from the tile terms a + b; g:
+// the cell of the walk, a guess of the exact cells). The trilinear march of a
+// cube holding negative values takes it for a cell next to a negative node:
+// there corners of both signs cancel, and an FP32 interpolation keeps only
+// ~1e-7 of the corners' size, while a run that ends at a zero crossing may
+// be short. Not inlined: it runs only in such cells.
+__device__ __noinline__ double samples_sum64(const CubeDev* Cp, const double* a, const double* b, double px,
+                                             double py, double pz, double dt, int i0, int i1, int g0, int g1,
+                                             int g2) {
+  double w[3], d[3];
+  for (int r = 0; r < 3; ++r) w[r] = __dadd_rn(a[r], b[r]);
+  dir64(w, d);
+  const double P[3] = {px, py, pz};
+  int g[3] = {g0, g1, g2};
+  double s = 0.0;
+  for (int i = i0; i < i1; ++i) s = __dadd_rn(s, sample_value64(*Cp, 1, d, P, dt, i, g));
+  return s;
 }
 
 // First sample in [lo, hi) of this lane's ray that is below zero (want_neg)
@@ -626,7 +658,9 @@ enum Axes { AXES_NONE = 0, AXES_DDA = 2, AXES_DDA_COMPACT = 3 };
 // map, the sample stride and the merge); the march itself is S-independent.
 // P: a CMEM model passed as a kernel parameter (nullptr: none); CMEM
 // requests whose model it is read its constants from the parameter space.
-template <int KIND, int INTERP, int AXES>
+// SIGNED: the trilinear march of a cube holding negative values, which sums
+// the cells next to a negative node in FP64 (samples_sum64).
+template <int KIND, int INTERP, int AXES, bool SIGNED = false>
 __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty, TileSmem& sm,
                                             KernelStats* stats, const CmemParam* P = nullptr) {
   const int SEGL2 = R.seg_log2;
@@ -963,7 +997,37 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           hi = __ldg(q + 1);
         }
         const float nxt = fminf(ceilf(fminf(fminf(ex[0], ex[1]), ex[2])), ub);
-        if (nxt > u) {
+        // a cube holding negative values: a cell next to a negative node
+        // (its flag) is summed sample by sample in the FP64 oracle's own
+        // arithmetic; its cell per axis is the walk table position
+        bool exact_cell_sum = false;
+        if constexpr (SIGNED) {
+          if (nxt > u) {
+            int cj[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              long long j;
+              if constexpr (COMPACT) j = signbit(d32[k]) ? C.walk4_dn[k] - wt[k] : wt[k] - C.walk4_up[k];
+              else j = signbit(d32[k]) ? C.walk_dn[k] - wt[k] : wt[k] - C.walk_up[k];
+              cj[k] = (int)min(max(j, 0ll), (long long)C.ax[k].n - 2);
+            }
+            long long fi = ((long long)cj[2] * C.ax[1].n + cj[1]) * C.ax[0].n + cj[0];
+#ifdef BIRP_DEBUG_BOUNDS
+            if (!bound_ok(fi, C.neg_n, 3)) fi = 0;
+#endif
+            if (__ldg(C.negflag + fi)) {
+              const double s64 = samples_sum64(R.cube, sm.A[lx], sm.B[ly], R.pos[0], R.pos[1], R.pos[2], R.dt,
+                                               first_c + (int)u, first_c + (int)nxt, cj[0], cj[1], cj[2]);
+              acc.add((float)s64);
+              u = nxt;
+              ++ncell;
+              exact_cell_sum = true;
+            }
+          }
+        }
+        if (exact_cell_sum) {
+          // summed above
+        } else if (nxt > u) {
           const float m = nxt - u;
           // pairs of independent FMAs as one packed FP32x2 instruction (the
           // record's float4 halves are the pairs: {c0, c3}, {c1, c5}, {c2,
@@ -1333,18 +1397,22 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 
 // One request, one CTA per tile; the request travels as a kernel parameter.
 // CMEM requests also get their model as a parameter.
-template <int KIND, int INTERP, int AXES>
+template <int KIND, int INTERP, int AXES, bool SIGNED = false>
 __global__ void __launch_bounds__(kThreads) render_plain_kernel(const __grid_constant__ RequestDev req,
                                                                 const __grid_constant__ CmemParam model,
                                                                 KernelStats* stats) {
   __shared__ TileSmem sm;
-  render_tile<KIND, INTERP, AXES>(req, blockIdx.x, blockIdx.y, sm, stats, KIND == SPACE_CMEM ? &model : nullptr);
+  render_tile<KIND, INTERP, AXES, SIGNED>(req, blockIdx.x, blockIdx.y, sm, stats,
+                                          KIND == SPACE_CMEM ? &model : nullptr);
 }
 
 // Dispatch over the request's variant.
 __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& sm, KernelStats* st) {
   if (R.kind == SPACE_CMEM) {
     render_tile<SPACE_CMEM, TRILINEAR, AXES_NONE>(R, tx, ty, sm, st);
+  } else if (R.interp && R.has_neg) {
+    if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true>(R, tx, ty, sm, st);
+    else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA, true>(R, tx, ty, sm, st);
   } else if (R.interp) {
     if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
     else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, st);
@@ -1359,7 +1427,9 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
 // queue head until the batch is exhausted. No waits: each CTA exits when the
 // queue is empty. Items are numbered in the host's order (largest work
 // first). CLS = BATCH_CUBE_TRI compiles only the trilinear cube march (fewer
-// registers, more resident warps); BATCH_ANY renders every request kind.
+// registers, more resident warps); BATCH_CUBE_SIGNED the trilinear march of
+// cubes holding negative values (either layout); BATCH_ANY renders every
+// request kind.
 // `model`: the CMEM class kernel reads this CMEM model's constants as
 // parameter operands for the requests that use it (model.dev).
 template <int CLS>
@@ -1367,6 +1437,7 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
                                            : CLS == BATCH_CMEM         ? BIRP_CMEM_MINB
                                            : CLS == BATCH_CUBE_NEAREST ? BIRP_NEAREST_MINB
                                            : CLS == BATCH_CUBE_TRI_COMPACT ? BIRP_COMPACT_MINB
+                                           : CLS == BATCH_CUBE_SIGNED  ? BIRP_SIGNED_MINB
                                                                        : BIRP_WALK_MINB)
     render_batch_kernel(BatchDev B, const __grid_constant__ CmemParam model) {
   __shared__ TileSmem sm;
@@ -1398,6 +1469,9 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
     } else if constexpr (CLS == BATCH_CUBE_NEAREST) {
       if (R.compact) render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
       else render_tile<SPACE_CUBE, NEAREST, AXES_DDA>(R, tx, ty, sm, B.stats);
+    } else if constexpr (CLS == BATCH_CUBE_SIGNED) {
+      if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true>(R, tx, ty, sm, B.stats);
+      else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA, true>(R, tx, ty, sm, B.stats);
     } else {
       render_tile_any(R, tx, ty, sm, B.stats);
     }
@@ -1699,6 +1773,10 @@ cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStr
     cp.dev = h.cmem;
   }
   if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_NONE><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else if (h.interp && h.has_neg && h.compact)
+    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else if (h.interp && h.has_neg)
+    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA, true><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.interp && h.compact)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, cp, stats);
@@ -1719,6 +1797,8 @@ int persistent_grid(int cls) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CMEM>, kThreads, 0);
   else if (cls == BATCH_CUBE_NEAREST)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_NEAREST>, kThreads, 0);
+  else if (cls == BATCH_CUBE_SIGNED)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_SIGNED>, kThreads, 0);
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_ANY>, kThreads, 0);
   if (per_sm < 1) per_sm = 1;
@@ -1732,6 +1812,7 @@ cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int
   else if (cls == BATCH_CUBE_TRI_COMPACT) render_batch_kernel<BATCH_CUBE_TRI_COMPACT><<<grid, kThreads, 0, s>>>(b, cp);
   else if (cls == BATCH_CMEM) render_batch_kernel<BATCH_CMEM><<<grid, kThreads, 0, s>>>(b, cp);
   else if (cls == BATCH_CUBE_NEAREST) render_batch_kernel<BATCH_CUBE_NEAREST><<<grid, kThreads, 0, s>>>(b, cp);
+  else if (cls == BATCH_CUBE_SIGNED) render_batch_kernel<BATCH_CUBE_SIGNED><<<grid, kThreads, 0, s>>>(b, cp);
   else render_batch_kernel<BATCH_ANY><<<grid, kThreads, 0, s>>>(b, cp);
   return cudaGetLastError();
 }
@@ -1741,6 +1822,7 @@ const void* render_batch_function(int cls) {
   if (cls == BATCH_CUBE_TRI_COMPACT) return (const void*)render_batch_kernel<BATCH_CUBE_TRI_COMPACT>;
   if (cls == BATCH_CMEM) return (const void*)render_batch_kernel<BATCH_CMEM>;
   if (cls == BATCH_CUBE_NEAREST) return (const void*)render_batch_kernel<BATCH_CUBE_NEAREST>;
+  if (cls == BATCH_CUBE_SIGNED) return (const void*)render_batch_kernel<BATCH_CUBE_SIGNED>;
   return (const void*)render_batch_kernel<BATCH_ANY>;
 }
 
