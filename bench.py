@@ -537,10 +537,14 @@ def run_profile_case(args):
                      ray_length=synth.RAY_LENGTH, trilinear=mode != "nearest") for p, a, nx, ny, s in reqs]
     items = [(space, c) for c in cams]
     batch = B.Batch(len(items), sum(c.nx * c.ny for c in cams))
+    B.kernel_stats(reset=True)
     for _ in range(args.launches):
         batch.submit(items)
         batch.wait()
-    print(json.dumps({"profile_case": mode, "requests": len(items), "last_launch_ms": batch.last_ms()[0]}))
+    ks = B.kernel_stats(reset=True)
+    print(json.dumps({"profile_case": mode, "requests": len(items), "last_launch_ms": batch.last_ms()[0],
+                      "cells_per_launch": ks["cells"] / args.launches,
+                      "samples_per_launch": ks["samples"] / args.launches}))
     batch.close()
 
 
