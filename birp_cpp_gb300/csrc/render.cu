@@ -1325,21 +1325,33 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     }
     n_exact_nearest = n_fp64;
   } else {
-    // Sample positions p + d ((i + 1/2) dt) from the ray's FP64 direction:
-    // the step d dt and the first position as float pairs (hi + lo), so a
-    // position is fma(i, st_hi, bs_hi) + fma(i, st_lo, bs_lo), within about
-    // one FP32 ulp of the FP64 position at any distance along the ray (an
-    // FP32 direction would put a sample t * 1e-7 Re off, a large relative
-    // error near the Earth, where the model's values are largest).
-    need_d64();
+    // Sample positions p + d ((i + 1/2) dt) from the ray's exact direction:
+    // the step d dt and the first position as float pairs (hi + lo, ~48-bit
+    // significands, from the tile's FP64 direction terms in float-float
+    // arithmetic as the nearest walk forms its crossings), so a position is
+    // fma(i, st_hi, bs_hi) + fma(i, st_lo, bs_lo), within about one FP32 ulp
+    // of the FP64 position at any distance along the ray (an FP32 direction
+    // would put a sample t * 1e-7 Re off, a large relative error near the
+    // Earth, where the model's values are largest).
     float st[3], bs[3], st_lo[3], bs_lo[3];
+    {
+      FF wf[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const double s64 = __dmul_rn(d64[k], R.dt), b64 = __dadd_rn(R.pos[k], __dmul_rn(0.5, s64));
-      st[k] = (float)s64;
-      st_lo[k] = (float)(s64 - (double)st[k]);
-      bs[k] = (float)b64;
-      bs_lo[k] = (float)(b64 - (double)bs[k]);
+      for (int k = 0; k < 3; ++k) {
+        const float h = (float)w64[k];
+        wf[k] = {h, (float)(w64[k] - (double)h)};
+      }
+      const FF rs = ff_rsqrt(ff_add(ff_add(ff_mul(wf[0], wf[0]), ff_mul(wf[1], wf[1])), ff_mul(wf[2], wf[2])));
+      const FF dtf = {R.dt_hi, R.dt_lo};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const FF s2 = ff_mul(ff_mul(wf[k], rs), dtf);
+        const FF b2 = ff_add({R.pos_hi[k], R.pos_lo[k]}, {0.5f * s2.hi, 0.5f * s2.lo});
+        st[k] = s2.hi;
+        st_lo[k] = s2.lo;
+        bs[k] = b2.hi;
+        bs_lo[k] = b2.lo;
+      }
     }
     // bound on |x32 - x64| of a sample: two FP32 roundings of a coordinate
     // (the reach of the ray bounds every coordinate) and the float pairs'
