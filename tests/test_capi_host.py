@@ -79,6 +79,25 @@ def test_frame_bitwise_equals_oracle(B, oracle, pos, aim):
         assert f[k] == g[k], k
 
 
+@pytest.mark.parametrize("roll", [-10.0, 3.25, 7.5])
+def test_frame_with_roll_bitwise_equals_oracle(B, oracle, roll):
+    """A roll offset (an extension; 0 is the reference's pose) gives the
+    oracle's frame bit for bit too, turns the frame by that angle about the
+    view axis, and leaves the Sun angle it is added to unchanged."""
+    pos, aim = (-2, -12, 16), (10, 0, 0)
+    cam = B.camera(pos, aim, 27.0, 16.0, 288, 168, n_samples=880, roll=roll)
+    f = B.camera_frame(cam)
+    g = oracle.frame64(oracle.camera64(pos, aim, 27.0, 16.0, 288, 168, 880, 44.0, 0, roll))
+    assert np.array_equal(f["rinv"], g["rinv"])
+    f0 = B.camera_frame(B.camera(pos, aim, 27.0, 16.0, 288, 168, n_samples=880))
+    assert f["angle_sun"] == f0["angle_sun"]
+    # the view axis (third column of R^-1, the -z camera axis) is unchanged;
+    # the image axes turn by the roll
+    assert np.allclose(f["rinv"][:, 2], f0["rinv"][:, 2], atol=1e-12)
+    c = float(np.dot(f["rinv"][:, 0], f0["rinv"][:, 0]))
+    assert abs(abs(c) - np.cos(np.radians(roll))) < 1e-12
+
+
 def test_frame_rotation_is_orthonormal(B):
     for pos, aim in POSES:
         f = B.camera_frame(B.camera(pos, aim, 27.0, 16.0, 64, 32))

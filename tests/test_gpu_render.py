@@ -40,7 +40,7 @@ def o_cube(oracle, c, tri):
 
 def o_cam(oracle, cam):
     return oracle.camera64(tuple(cam.pos), tuple(cam.aim), cam.fov_w_deg, cam.fov_h_deg, cam.nx, cam.ny,
-                           cam.n_samples, cam.ray_length, cam.march)
+                           cam.n_samples, cam.ray_length, cam.march, cam.roll_deg)
 
 
 def test_constant_field_counts_are_exact(birp, oracle):
@@ -176,6 +176,46 @@ def test_cmem_render(birp, oracle):
         ref = oracle.render64(om, o_cam(oracle, cam), threads=THREADS)
         mx, rms, n = rel_err(img, ref)
         assert mx <= TOL, (pos, mx, rms)
+
+
+@pytest.mark.parametrize("roll", [-10.0, 6.5])
+def test_roll(birp, oracle, cube1, roll):
+    """A camera rolled about its view axis (an extension; the benchmark draws
+    the roll U[-10, 10] deg): cube and CMEM against the FP64 oracle."""
+    for pos in [(-2, -12, 16), (3.49, 0.0746, 0.244)]:
+        cam = birp.camera(pos, (9, 0, 0), 27.0, 16.0, 80, 48, n_samples=880, roll=roll)
+        img = birp.render(cube1["gpu"], cam)
+        ref = oracle.render64(o_cube(oracle, cube1, True), o_cam(oracle, cam), threads=THREADS)
+        mx, rms, n = rel_err(img, ref)
+        assert mx <= TOL, (pos, roll, mx)
+        flat = birp.render(cube1["gpu"], birp.camera(pos, (9, 0, 0), 27.0, 16.0, 80, 48, n_samples=880))
+        assert not np.array_equal(img, flat)
+    m = birp.Cmem()
+    cam = birp.camera((-2, -12, 16), (10, 0, 0), 27.0, 16.0, 72, 42, n_samples=440, roll=roll)
+    mx, rms, n = rel_err(birp.render(m, cam), oracle.render64(oracle.Cmem64(), o_cam(oracle, cam), threads=THREADS))
+    assert mx <= TOL, (roll, mx)
+    m.close()
+
+
+def test_cmem_near_earth_cusp(birp, oracle):
+    """Two orbit views (config 3's CMEM requests 1 and 4) whose rays pass the
+    Earth inside the cusps, where the cusp term cancels most of the
+    magnetopause radius (down to ~0.2 Re) and the model is ill-conditioned:
+    before float-pair sample positions and the FP64 path for such ramp
+    samples, their worst pixels were 4e-3 and 6e-5 off the FP64 oracle.
+    Whole images, within the path's 1e-5."""
+    from birp_cpp_gb300 import synth
+    _, specs = synth.config3_specs()
+    cmem = [s for s in specs if s[0] < 0]
+    m = birp.Cmem()
+    om = oracle.Cmem64()
+    for _, pos, aim, nx, ny, step in (cmem[1], cmem[4]):
+        cam = birp.camera(pos, aim, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(step))
+        img = birp.render(m, cam)
+        ref = oracle.render64(om, o_cam(oracle, cam), threads=THREADS)
+        mx, rms, n = rel_err(img, ref)
+        assert mx <= TOL, (pos, mx, rms, n)
+    m.close()
 
 
 def test_cmem_margin_holds(birp):
