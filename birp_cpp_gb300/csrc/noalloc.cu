@@ -25,6 +25,7 @@ constexpr size_t kOffOrder = kOffFirst + (kNoAllocMaxRequests + 1) * sizeof(int)
 constexpr size_t kOffReqs = (kOffOrder + kNoAllocMaxRequests * sizeof(int) + 15) / 16 * 16;
 constexpr size_t kOffCounter = kOffReqs + kNoAllocMaxRequests * sizeof(RequestDev);
 constexpr size_t kScratchBytes = (kOffCounter + sizeof(unsigned int) + 255) / 256 * 256;
+static_assert(kScratchBytes <= 70000, "the array's size as the header states it (70 KB)");
 
 // The scratch of every call. In host code this name is only a stand-in for
 // the symbol: its device address comes from cudaGetSymbolAddress.

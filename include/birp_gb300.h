@@ -206,7 +206,7 @@ birp_status birp_batch_render(birp_batch* b, const birp_request* reqs, int n, fl
  * inside another framework's operator, where that framework owns the device
  * memory; loops that must not allocate). The caller passes the requests and
  * one DEVICE output buffer of ny*nx floats per request; the only other device
- * memory used is a 64 KB array inside this library (held on every GPU that
+ * memory used is a 70 KB array inside this library (held on every GPU that
  * loads it), set up by the first call on each device (make that first call
  * before any stream capture). Runs on the library's device (birp_init), as
  * the other entry points, from any host thread. Asynchronous on `stream`
