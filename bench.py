@@ -370,9 +370,10 @@ def run_c4(args, B, O):
     t_setup = time.perf_counter()
     xs, ys, zs, bases = synth.serving_bases(nx, ny, nz)
     layout = B.CUBE_COMPACT if args.c4_layout == "compact" else B.CUBE_RECORDS
+    records_share = int(args.c4_records_gb * (1 << 30)) if layout == B.CUBE_COMPACT else 0
     srv = B.Server(B.server_config(cube_budget_bytes=int(args.c4_budget_gb * (1 << 30)), slots=3,
                                    max_batch_requests=64, max_batch_pixels=16 << 20, max_wait_ms=1.0,
-                                   max_queue=1 << 17, cube_layout=layout))
+                                   max_queue=1 << 17, cube_layout=layout, records_budget_bytes=records_share))
 
     def add(i):
         return srv.add_cube(xs, ys, zs, synth.serving_cube(i, bases))
@@ -516,8 +517,11 @@ def run_c4(args, B, O):
     cube.close()
     return {"workload": f"config 4 serving sweep: {n_cubes} cubes of {nx}x{ny}x{nz} FP32 "
                         f"({n_cubes * nx * ny * nz * 4 / 1e9:.1f} GB of pinned host copies), Zipf(1.1) popularity, "
-                        f"{args.c4_budget_gb:g} GiB device budget, {args.c4_layout} layout, Poisson arrivals, "
-                        f"{args.c4_seconds:g} s per offered rate (70% run: {2 * args.c4_seconds:g} s)",
+                        f"{args.c4_budget_gb:g} GiB device budget, {args.c4_layout} layout"
+                        + (f" (up to {args.c4_records_gb:g} GiB of it for the most-requested cubes, promoted to "
+                           f"the records layout)" if records_share else "")
+                        + f", Poisson arrivals, {args.c4_seconds:g} s per offered rate (70% run: "
+                          f"{2 * args.c4_seconds:g} s)",
             "cube_device_bytes": cube_bytes,
             "resident_cubes_in_budget": int(args.c4_budget_gb * (1 << 30) // max(cube_bytes, 1)),
             "setup_s": setup_s, "warm_s": warm_s, "warm_uploads": int(st_warm.cube_uploads),
@@ -525,6 +529,8 @@ def run_c4(args, B, O):
             "gpu_batched_one_cube_images_s": ceiling,
             "at_70pct_of_saturation": at70,
             "uploads_total": int(st_end.cube_uploads), "evictions_total": int(st_end.cube_evictions),
+            "records_share_gb": args.c4_records_gb if records_share else 0,
+            "promotions_to_records": int(st_end.cube_promotions), "records_bytes_end": int(st_end.records_bytes),
             "plain": {"p50_ms": float(np.percentile(pl, 50)), "p99_ms": float(np.percentile(pl, 99)),
                       "images_s": len(pl) / (sum(pl) / 1000)},
             "parity": parity}
@@ -686,6 +692,8 @@ def main():
     ap.add_argument("--c4-seconds", type=float, default=4.0)
     ap.add_argument("--c4-layout", default="compact", choices=["compact", "records"],
                     help="device layout of the served cubes")
+    ap.add_argument("--c4-records-gb", type=float, default=10.0,
+                    help="share of the budget for cubes the server promotes to the records layout (0: none)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.requests is None:

@@ -58,7 +58,7 @@ class CubeInfo(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("cube_budget_bytes", C.c_int64), ("slots", C.c_int), ("max_batch_requests", C.c_int),
                 ("max_batch_pixels", C.c_int64), ("max_queue", C.c_int), ("max_wait_ms", C.c_double),
-                ("cube_layout", C.c_int)]
+                ("cube_layout", C.c_int), ("records_budget_bytes", C.c_int64)]
 
 
 class Result(C.Structure):
@@ -68,7 +68,8 @@ class Result(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "rejected", "batches", "cube_uploads",
-                                         "cube_evictions", "cube_hits", "resident_bytes")]
+                                         "cube_evictions", "cube_hits", "resident_bytes", "cube_promotions",
+                                         "records_bytes")]
 
 
 class KernelStats(C.Structure):

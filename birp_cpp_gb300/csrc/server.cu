@@ -47,6 +47,9 @@ struct Source {
   bool uploading = false;   // queued for or in the uploader
   birp_status upload_err = BIRP_OK;  // the last upload's failure, reported once
   birp_cmem* cmem = nullptr;
+  int64_t requests = 0;       // requests submitted for it (the promotion's ranking)
+  int64_t bytes_records = 0;  // device bytes in the records layout
+  bool promoting = false;     // its records copy is being built
 };
 
 struct Req {
@@ -63,6 +66,7 @@ struct Slot {
   birp_batch* batch = nullptr;
   std::vector<Req*> reqs;
   std::vector<int> srcs;  // distinct sources pinned by this batch
+  std::vector<birp_cube*> cubes;  // the device cubes its requests read
   bool busy = false;
   bool has_work = false;
   std::condition_variable cv;
@@ -86,6 +90,10 @@ struct birp_server {
   int64_t next_ticket = 1;
   uint64_t tick = 0;
   int64_t resident_bytes = 0;
+  int64_t records_bytes = 0;  // resident cubes promoted to the records layout
+  // compact copies replaced by their records copy while batches in flight
+  // still read them: freed when the last of those batches completes
+  std::vector<std::pair<birp_cube*, int>> retired;
   cudaStream_t upload_stream = nullptr;
   birp_server_stats st{};
 };
@@ -98,31 +106,101 @@ void finish(birp_server*, Req* r, birp_status status) {
   r->done = true;
 }
 
-// Frees budget for source `id` by evicting least-recently-used resident
-// cubes that no batch references; called with the lock held. BIRP_ERR_BUSY
-// when the budget is held by in-flight batches (retry later).
-birp_status make_room(birp_server* s, int id) {
-  Source& src = s->sources[id];
-  if (src.bytes > s->cfg.cube_budget_bytes)
-    return fail(BIRP_ERR_NOMEM, "cube needs %lld B, budget is %lld B", (long long)src.bytes,
+// Frees budget for `need` more bytes by evicting least-recently-used
+// resident cubes (other than source `keep`) that no batch references; called
+// with the lock held. BIRP_ERR_BUSY when the budget is held by in-flight
+// batches (retry later).
+birp_status make_room_bytes(birp_server* s, int64_t need, int keep) {
+  if (need > s->cfg.cube_budget_bytes)
+    return fail(BIRP_ERR_NOMEM, "cube needs %lld B, budget is %lld B", (long long)need,
                 (long long)s->cfg.cube_budget_bytes);
-  while (s->resident_bytes + src.bytes > s->cfg.cube_budget_bytes) {
+  while (s->resident_bytes + need > s->cfg.cube_budget_bytes) {
     int victim = -1;
     for (int i = 0; i < (int)s->sources.size(); ++i) {
       const Source& o = s->sources[i];
-      if (i == id || !o.resident || o.in_use > 0) continue;
+      if (i == keep || !o.resident || o.in_use > 0 || o.promoting) continue;
       if (victim < 0 || o.last_use < s->sources[victim].last_use) victim = i;
     }
     if (victim < 0) return BIRP_ERR_BUSY;
     Source& v = s->sources[victim];
     birp_cube* c = v.resident;
     v.resident = nullptr;
-    s->resident_bytes -= v.bytes;
+    s->resident_bytes -= (int64_t)c->device_bytes;
+    if (c->layout == BIRP_CUBE_RECORDS && s->cfg.records_budget_bytes > 0) s->records_bytes -= (int64_t)c->device_bytes;
     s->st.cube_evictions++;
     destroy_cube_device(*c);  // stream-ordered release on the upload stream
     delete c;
   }
   return BIRP_OK;
+}
+
+birp_status make_room(birp_server* s, int id) { return make_room_bytes(s, s->sources[id].bytes, id); }
+
+// A cube that batches in flight may still read is freed once the last of
+// them completes (called with the lock held).
+void retire_cube(birp_server* s, birp_cube* c) {
+  int refs = 0;
+  for (Slot* sl : s->slots)
+    if (sl->busy && std::find(sl->cubes.begin(), sl->cubes.end(), c) != sl->cubes.end()) ++refs;
+  if (refs == 0) {
+    s->resident_bytes -= (int64_t)c->device_bytes;
+    destroy_cube_device(*c);
+    delete c;
+  } else {
+    s->retired.push_back({c, refs});
+  }
+}
+
+// Promotion (records_budget_bytes > 0; uploader thread, lock held on entry
+// and exit): the most-requested resident compact cube whose records copy
+// fits the records share is rebuilt in the records layout from its host
+// copy, with the lock released meanwhile, and takes the compact copy's
+// place. Returns whether it did one.
+bool try_promote(birp_server* s, std::unique_lock<std::mutex>& lk) {
+  if (s->cfg.records_budget_bytes <= 0 || s->cfg.cube_layout != BIRP_CUBE_COMPACT) return false;
+  int best = -1;
+  for (int i = 0; i < (int)s->sources.size(); ++i) {
+    const Source& o = s->sources[i];
+    if (o.kind != 0 || !o.resident || o.resident->layout != BIRP_CUBE_COMPACT || o.uploading || o.promoting ||
+        o.requests < 16 || s->records_bytes + o.bytes_records > s->cfg.records_budget_bytes)
+      continue;
+    if (best < 0 || o.requests > s->sources[best].requests) best = i;
+  }
+  if (best < 0) return false;
+  // room for the records copy beside the compact one until the swap
+  if (make_room_bytes(s, s->sources[best].bytes_records, best) != BIRP_OK) return false;
+  Source& src = s->sources[best];
+  src.promoting = true;
+  const int64_t reserved = src.bytes_records;
+  s->resident_bytes += reserved;
+  const float* vals = src.h_vals;
+  const int has_neg = src.has_neg;
+  std::vector<double> ax[3] = {src.ax[0], src.ax[1], src.ax[2]};
+  lk.unlock();
+  birp_cube* c = new birp_cube();
+  c->layout = BIRP_CUBE_RECORDS;
+  c->has_neg = has_neg;
+  birp_status rc = BIRP_OK;
+  for (int k = 0; k < 3 && rc == BIRP_OK; ++k) rc = analyze_axis(ax[k].data(), (int)ax[k].size(), "xyz"[k], *c, k);
+  if (rc == BIRP_OK) rc = upload_cube(*c, vals, s->upload_stream, true);
+  lk.lock();
+  Source& done = s->sources[best];  // (the vector may have grown meanwhile)
+  s->resident_bytes -= reserved;
+  done.promoting = false;
+  if (rc != BIRP_OK || !done.resident) {
+    destroy_cube_device(*c);
+    delete c;
+    return false;
+  }
+  s->resident_bytes += (int64_t)c->device_bytes;
+  s->records_bytes += (int64_t)c->device_bytes;
+  done.bytes_records = (int64_t)c->device_bytes;
+  birp_cube* old = done.resident;
+  done.resident = c;  // batches formed from now on read the records copy
+  done.bytes = (int64_t)c->device_bytes;
+  retire_cube(s, old);
+  s->st.cube_promotions++;
+  return true;
 }
 
 // Uploader thread: makes the queued cubes resident one at a time, with the
@@ -132,7 +210,11 @@ void uploader_loop(birp_server* s) {
   std::unique_lock<std::mutex> lk(s->mu);
   while (!s->stop) {
     if (s->upload_q.empty()) {
-      s->cv_upload.wait(lk);
+      // idle: promote a popular compact cube, else wait for work (and look
+      // again for a promotion now and then)
+      if (try_promote(s, lk)) continue;
+      if (s->cfg.records_budget_bytes > 0) s->cv_upload.wait_for(lk, std::chrono::milliseconds(20));
+      else s->cv_upload.wait(lk);
       continue;
     }
     const int id = s->upload_q.front();
@@ -194,8 +276,19 @@ void slot_worker(birp_server* s, Slot* slot) {
     for (Req* r : slot->reqs) finish(s, r, rc);
     s->st.completed += (int64_t)slot->reqs.size();
     for (int id : slot->srcs) s->sources[id].in_use--;
+    // replaced cubes this batch still read: free the last reader's
+    for (birp_cube* c : slot->cubes)
+      for (size_t k = 0; k < s->retired.size(); ++k)
+        if (s->retired[k].first == c && --s->retired[k].second == 0) {
+          s->resident_bytes -= (int64_t)c->device_bytes;
+          destroy_cube_device(*c);
+          delete c;
+          s->retired.erase(s->retired.begin() + (long)k);
+          break;
+        }
     slot->reqs.clear();
     slot->srcs.clear();
+    slot->cubes.clear();
     slot->has_work = false;
     slot->busy = false;
     s->cv_done.notify_all();
@@ -304,12 +397,16 @@ void scheduler_loop(birp_server* s) {
     s->st.batches++;
     slot->reqs = go;
     slot->srcs = used_srcs;
+    slot->cubes.clear();
+    for (int id : used_srcs)
+      if (s->sources[id].kind == 0) slot->cubes.push_back(s->sources[id].resident);
     if (rc != BIRP_OK) {
       for (Req* r : go) finish(s, r, rc);
       s->st.completed += (int64_t)go.size();
       for (int id : used_srcs) s->sources[id].in_use--;
       slot->reqs.clear();
       slot->srcs.clear();
+      slot->cubes.clear();
       slot->busy = false;
       s->cv_done.notify_all();
       continue;
@@ -332,6 +429,7 @@ void birp_server_default_config(birp_server_config* c) {
   c->max_queue = 1 << 16;
   c->max_wait_ms = 1.0;
   c->cube_layout = BIRP_CUBE_RECORDS;
+  c->records_budget_bytes = 0;
 }
 
 birp_status birp_server_create(const birp_server_config* cfg, birp_server** out) {
@@ -343,7 +441,8 @@ birp_status birp_server_create(const birp_server_config* cfg, birp_server** out)
   if (cfg) c = *cfg;
   if (c.slots < 1 || c.slots > 16 || c.max_batch_requests < 1 || c.max_batch_pixels < 1 || c.max_queue < 1 ||
       c.cube_budget_bytes < 0 || !(c.max_wait_ms >= 0) ||
-      (c.cube_layout != BIRP_CUBE_RECORDS && c.cube_layout != BIRP_CUBE_COMPACT))
+      (c.cube_layout != BIRP_CUBE_RECORDS && c.cube_layout != BIRP_CUBE_COMPACT) || c.records_budget_bytes < 0 ||
+      c.records_budget_bytes > c.cube_budget_bytes)
     return fail(BIRP_ERR_INVALID, "bad server configuration");
   birp_server* s = new birp_server();
   s->cfg = c;
@@ -403,6 +502,11 @@ birp_status birp_server_destroy(birp_server* s) {
   for (Req* r : s->pending) delete r;
   for (auto& kv : s->tickets)
     if (std::find(s->pending.begin(), s->pending.end(), kv.second) == s->pending.end()) delete kv.second;
+  for (auto& rc : s->retired) {
+    destroy_cube_device(*rc.first);
+    delete rc.first;
+  }
+  s->retired.clear();
   for (Source& src : s->sources) {
     if (src.resident) {
       destroy_cube_device(*src.resident);
@@ -437,6 +541,9 @@ birp_status birp_server_add_cube(birp_server* s, const double* xs, int nx, const
   std::memcpy(src.h_vals, values, count * sizeof(float));
   src.has_neg = probe.has_neg = any_negative(src.h_vals, count) ? 1 : 0;
   src.bytes = (int64_t)cube_device_bytes(probe);
+  birp_cube probe_records = probe;
+  probe_records.layout = BIRP_CUBE_RECORDS;
+  src.bytes_records = (int64_t)cube_device_bytes(probe_records);
   std::lock_guard<std::mutex> lk(s->mu);
   s->sources.push_back(std::move(src));
   *cube_id = (int)s->sources.size() - 1;
@@ -464,6 +571,7 @@ birp_status birp_server_submit(birp_server* s, int source_id, const birp_camera*
     s->st.rejected++;
     return fail(BIRP_ERR_BUSY, "queue full (%d pending)", (int)s->pending.size());
   }
+  s->sources[source_id].requests++;
   Req* r = new Req();
   r->ticket = s->next_ticket++;
   r->src = source_id;
@@ -508,6 +616,7 @@ birp_status birp_server_get_stats(const birp_server* s, birp_server_stats* out) 
   std::lock_guard<std::mutex> lk(m->mu);
   *out = m->st;
   out->resident_bytes = m->resident_bytes;
+  out->records_bytes = m->records_bytes;
   return ok();
 }
 

@@ -252,6 +252,14 @@ typedef struct {
   int max_queue;               /* pending requests before submit returns BIRP_ERR_BUSY */
   double max_wait_ms;          /* batching window: launch when this old or the batch is full */
   int cube_layout;             /* device layout of the server's cubes (BIRP_CUBE_*) */
+  /* With cube_layout = BIRP_CUBE_COMPACT: the part of cube_budget_bytes that
+   * cubes promoted to the records layout (about 8x the memory, 1.35x faster
+   * to render) may hold; 0 = no promotion. When no upload is waiting, the
+   * most-requested resident compact cube (at least 16 requests) whose
+   * records copy fits that share is rebuilt in the records layout from its
+   * host copy and takes the compact copy's place; the compact copy is freed
+   * once no batch in flight uses it. No counterpart in the reference. */
+  int64_t records_budget_bytes;
 } birp_server_config;
 
 typedef struct {
@@ -265,6 +273,8 @@ typedef struct {
   int64_t submitted, completed, rejected, batches;
   int64_t cube_uploads, cube_evictions, cube_hits;
   int64_t resident_bytes;
+  int64_t cube_promotions;     /* compact cubes rebuilt in the records layout */
+  int64_t records_bytes;       /* GPU bytes the promoted cubes hold now */
 } birp_server_stats;
 
 void birp_server_default_config(birp_server_config* c);
