@@ -373,7 +373,8 @@ def run_c4(args, B, O):
     records_share = int(args.c4_records_gb * (1 << 30)) if layout == B.CUBE_COMPACT else 0
     srv = B.Server(B.server_config(cube_budget_bytes=int(args.c4_budget_gb * (1 << 30)), slots=3,
                                    max_batch_requests=64, max_batch_pixels=16 << 20, max_wait_ms=1.0,
-                                   max_queue=1 << 17, cube_layout=layout, records_budget_bytes=records_share))
+                                   max_queue=1 << 17, cube_layout=layout, records_budget_bytes=records_share,
+                                   uploaders=args.c4_uploaders))
 
     def add(i):
         return srv.add_cube(xs, ys, zs, synth.serving_cube(i, bases))
@@ -529,7 +530,7 @@ def run_c4(args, B, O):
             "gpu_batched_one_cube_images_s": ceiling,
             "at_70pct_of_saturation": at70,
             "uploads_total": int(st_end.cube_uploads), "evictions_total": int(st_end.cube_evictions),
-            "records_share_gb": args.c4_records_gb if records_share else 0,
+            "records_share_gb": args.c4_records_gb if records_share else 0, "uploaders": args.c4_uploaders,
             "promotions_to_records": int(st_end.cube_promotions), "records_bytes_end": int(st_end.records_bytes),
             "plain": {"p50_ms": float(np.percentile(pl, 50)), "p99_ms": float(np.percentile(pl, 99)),
                       "images_s": len(pl) / (sum(pl) / 1000)},
@@ -692,7 +693,8 @@ def main():
     ap.add_argument("--c4-seconds", type=float, default=4.0)
     ap.add_argument("--c4-layout", default="compact", choices=["compact", "records"],
                     help="device layout of the served cubes")
-    ap.add_argument("--c4-records-gb", type=float, default=10.0,
+    ap.add_argument("--c4-uploaders", type=int, default=2, help="the server's parallel cube uploads")
+    ap.add_argument("--c4-records-gb", type=float, default=0.0,
                     help="share of the budget for cubes the server promotes to the records layout (0: none)")
     args = ap.parse_args()
     world, rank, local = dist_setup()

@@ -58,7 +58,7 @@ class CubeInfo(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("cube_budget_bytes", C.c_int64), ("slots", C.c_int), ("max_batch_requests", C.c_int),
                 ("max_batch_pixels", C.c_int64), ("max_queue", C.c_int), ("max_wait_ms", C.c_double),
-                ("cube_layout", C.c_int), ("records_budget_bytes", C.c_int64)]
+                ("cube_layout", C.c_int), ("records_budget_bytes", C.c_int64), ("uploaders", C.c_int)]
 
 
 class Result(C.Structure):

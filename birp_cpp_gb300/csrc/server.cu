@@ -4,11 +4,13 @@
 // the pending queue whenever a slot (a batch object with its own stream and
 // CUDA graph) is free, taking requests whose source is resident. Cubes live in
 // GPU memory under a byte budget; a request for a cube that is not resident
-// waits while an uploader thread brings the cube in (evicting
+// waits while one of the uploader threads brings the cube in (evicting
 // least-recently-used cubes that no in-flight batch references, re-uploading
-// from the pinned host copy on a separate stream, with stream-ordered pool
-// allocations so neither upload nor eviction synchronises the device) — the
-// other requests keep being batched meanwhile. Batches on different slots
+// from the pinned host copy on that uploader's own stream, with
+// stream-ordered pool allocations so neither upload nor eviction
+// synchronises the device) — the other requests keep being batched
+// meanwhile. With a records share, an idle uploader rebuilds the most
+// requested compact cube in the records layout. Batches on different slots
 // overlap on the GPU. One completion thread per slot waits for its batch,
 // copies each image to the caller's buffer unless the kernels wrote it there,
 // and completes the tickets.
@@ -81,7 +83,7 @@ struct birp_server {
   std::condition_variable cv_sched, cv_done, cv_upload;
   std::deque<Req*> pending;
   std::deque<int> upload_q;  // sources to make resident, in request order
-  std::thread uploader;
+  std::vector<std::thread> uploaders;  // one stream each (upload_streams)
   std::unordered_map<int64_t, Req*> tickets;
   std::vector<Source> sources;
   std::vector<Slot*> slots;
@@ -94,7 +96,7 @@ struct birp_server {
   // compact copies replaced by their records copy while batches in flight
   // still read them: freed when the last of those batches completes
   std::vector<std::pair<birp_cube*, int>> retired;
-  cudaStream_t upload_stream = nullptr;
+  std::vector<cudaStream_t> upload_streams;
   birp_server_stats st{};
 };
 
@@ -156,7 +158,7 @@ void retire_cube(birp_server* s, birp_cube* c) {
 // fits the records share is rebuilt in the records layout from its host
 // copy, with the lock released meanwhile, and takes the compact copy's
 // place. Returns whether it did one.
-bool try_promote(birp_server* s, std::unique_lock<std::mutex>& lk) {
+bool try_promote(birp_server* s, std::unique_lock<std::mutex>& lk, cudaStream_t stream) {
   if (s->cfg.records_budget_bytes <= 0 || s->cfg.cube_layout != BIRP_CUBE_COMPACT) return false;
   int best = -1;
   for (int i = 0; i < (int)s->sources.size(); ++i) {
@@ -182,7 +184,7 @@ bool try_promote(birp_server* s, std::unique_lock<std::mutex>& lk) {
   c->has_neg = has_neg;
   birp_status rc = BIRP_OK;
   for (int k = 0; k < 3 && rc == BIRP_OK; ++k) rc = analyze_axis(ax[k].data(), (int)ax[k].size(), "xyz"[k], *c, k);
-  if (rc == BIRP_OK) rc = upload_cube(*c, vals, s->upload_stream, true);
+  if (rc == BIRP_OK) rc = upload_cube(*c, vals, stream, true);
   lk.lock();
   Source& done = s->sources[best];  // (the vector may have grown meanwhile)
   s->resident_bytes -= reserved;
@@ -203,16 +205,19 @@ bool try_promote(birp_server* s, std::unique_lock<std::mutex>& lk) {
   return true;
 }
 
-// Uploader thread: makes the queued cubes resident one at a time, with the
-// lock released during the upload itself, and wakes the scheduler.
-void uploader_loop(birp_server* s) {
+// Uploader threads (`uploaders` of them, each with its own stream): each
+// makes queued cubes resident one at a time, with the lock released during
+// the upload itself, and wakes the scheduler; several uploads proceed at
+// once.
+void uploader_loop(birp_server* s, int idx) {
   cudaSetDevice(g_ctx.device);  // per host thread
+  const cudaStream_t stream = s->upload_streams[idx];
   std::unique_lock<std::mutex> lk(s->mu);
   while (!s->stop) {
     if (s->upload_q.empty()) {
       // idle: promote a popular compact cube, else wait for work (and look
       // again for a promotion now and then)
-      if (try_promote(s, lk)) continue;
+      if (try_promote(s, lk, stream)) continue;
       if (s->cfg.records_budget_bytes > 0) s->cv_upload.wait_for(lk, std::chrono::milliseconds(20));
       else s->cv_upload.wait(lk);
       continue;
@@ -236,7 +241,7 @@ void uploader_loop(birp_server* s) {
       lk.unlock();
       for (int k = 0; k < 3 && rc == BIRP_OK; ++k)
         rc = analyze_axis(ax[k].data(), (int)ax[k].size(), "xyz"[k], *c, k);
-      if (rc == BIRP_OK) rc = upload_cube(*c, vals, s->upload_stream, true);
+      if (rc == BIRP_OK) rc = upload_cube(*c, vals, stream, true);
       lk.lock();
       Source& done = s->sources[id];  // (the vector may have grown meanwhile)
       s->resident_bytes -= reserved;
@@ -430,6 +435,7 @@ void birp_server_default_config(birp_server_config* c) {
   c->max_wait_ms = 1.0;
   c->cube_layout = BIRP_CUBE_RECORDS;
   c->records_budget_bytes = 0;
+  c->uploaders = 2;
 }
 
 birp_status birp_server_create(const birp_server_config* cfg, birp_server** out) {
@@ -442,14 +448,19 @@ birp_status birp_server_create(const birp_server_config* cfg, birp_server** out)
   if (c.slots < 1 || c.slots > 16 || c.max_batch_requests < 1 || c.max_batch_pixels < 1 || c.max_queue < 1 ||
       c.cube_budget_bytes < 0 || !(c.max_wait_ms >= 0) ||
       (c.cube_layout != BIRP_CUBE_RECORDS && c.cube_layout != BIRP_CUBE_COMPACT) || c.records_budget_bytes < 0 ||
-      c.records_budget_bytes > c.cube_budget_bytes)
+      c.records_budget_bytes > c.cube_budget_bytes || c.uploaders < 1 || c.uploaders > 8)
     return fail(BIRP_ERR_INVALID, "bad server configuration");
   birp_server* s = new birp_server();
   s->cfg = c;
-  cudaError_t e = cudaStreamCreateWithFlags(&s->upload_stream, cudaStreamNonBlocking);
-  if (e != cudaSuccess) {
-    delete s;
-    return fail(BIRP_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+  for (int i = 0; i < c.uploaders; ++i) {
+    cudaStream_t us = nullptr;
+    cudaError_t e = cudaStreamCreateWithFlags(&us, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      for (cudaStream_t u : s->upload_streams) cudaStreamDestroy(u);
+      delete s;
+      return fail(BIRP_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+    }
+    s->upload_streams.push_back(us);
   }
   // keep freed cube memory in the process's pool for reuse (no release to the
   // driver between evictions); a per-process setting of this library's pool
@@ -469,7 +480,7 @@ birp_status birp_server_create(const birp_server_config* cfg, birp_server** out)
     s->slots.push_back(sl);
   }
   for (Slot* sl : s->slots) sl->worker = std::thread(slot_worker, s, sl);
-  s->uploader = std::thread(uploader_loop, s);
+  for (int i = 0; i < c.uploaders; ++i) s->uploaders.emplace_back(uploader_loop, s, i);
   s->scheduler = std::thread(scheduler_loop, s);
   *out = s;
   return ok();
@@ -485,7 +496,8 @@ birp_status birp_server_destroy(birp_server* s) {
     for (Slot* sl : s->slots) sl->cv.notify_all();
   }
   if (s->scheduler.joinable()) s->scheduler.join();
-  if (s->uploader.joinable()) s->uploader.join();
+  for (std::thread& u : s->uploaders)
+    if (u.joinable()) u.join();
   for (Slot* sl : s->slots) {
     // a batch still in flight is waited for by its worker before it exits
     {
@@ -515,9 +527,9 @@ birp_status birp_server_destroy(birp_server* s) {
     if (src.h_vals) cudaFreeHost(src.h_vals);
     if (src.cmem) birp_cmem_destroy(src.cmem);
   }
-  if (s->upload_stream) {
-    cudaStreamSynchronize(s->upload_stream);
-    cudaStreamDestroy(s->upload_stream);
+  for (cudaStream_t u : s->upload_streams) {
+    cudaStreamSynchronize(u);
+    cudaStreamDestroy(u);
   }
   delete s;
   return ok();

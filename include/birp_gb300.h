@@ -260,6 +260,7 @@ typedef struct {
    * host copy and takes the compact copy's place; the compact copy is freed
    * once no batch in flight uses it. No counterpart in the reference. */
   int64_t records_budget_bytes;
+  int uploaders;               /* cube uploads in parallel (1..8; one stream each) */
 } birp_server_config;
 
 typedef struct {
