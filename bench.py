@@ -693,7 +693,7 @@ def main():
     ap.add_argument("--c4-seconds", type=float, default=4.0)
     ap.add_argument("--c4-layout", default="compact", choices=["compact", "records"],
                     help="device layout of the served cubes")
-    ap.add_argument("--c4-uploaders", type=int, default=2, help="the server's parallel cube uploads")
+    ap.add_argument("--c4-uploaders", type=int, default=1, help="the server's parallel cube uploads")
     ap.add_argument("--c4-records-gb", type=float, default=0.0,
                     help="share of the budget for cubes the server promotes to the records layout (0: none)")
     args = ap.parse_args()

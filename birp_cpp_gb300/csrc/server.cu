@@ -435,7 +435,7 @@ void birp_server_default_config(birp_server_config* c) {
   c->max_wait_ms = 1.0;
   c->cube_layout = BIRP_CUBE_RECORDS;
   c->records_budget_bytes = 0;
-  c->uploaders = 2;
+  c->uploaders = 1;
 }
 
 birp_status birp_server_create(const birp_server_config* cfg, birp_server** out) {
