@@ -192,6 +192,38 @@ static void concurrent_cameras() {
   CHECK(mx > 0);
 }
 
+// The roll extension: SetRoll(0) is the reference's pose (the same image
+// bit for bit); a roll turns the image (a different one, not empty).
+static void camera_roll() {
+  std::vector<double> xs, ys, zs;
+  for (int i = 0; i < 40; ++i) xs.push_back(-10 + 30.0 * i / 39);
+  for (int i = 0; i < 32; ++i) ys.push_back(-15 + 30.0 * i / 31);
+  for (int i = 0; i < 24; ++i) zs.push_back(-15 + 30.0 * i / 23);
+  std::vector<float> vals;
+  for (int k = 0; k < 24; ++k)
+    for (int j = 0; j < 32; ++j)
+      for (int i = 0; i < 40; ++i) vals.push_back(1.0f + 0.02f * ((i * 5 + j * 11 + k * 17) % 89));
+  DataCube cube;
+  cube.Init(xs, ys, zs, vals);
+  cube.SetTrilinear(true);
+  auto render = [&cube](double roll, bool set) {
+    Camera cam(cube, 16.f, 27.f, 48, 28);
+    float px = 1.f, py = -5.f, pz = 4.f;
+    cam.SetPosition(px, py, pz);
+    cam.SetAim(10.f, 0.f, 0.f);
+    if (set) cam.SetRoll(roll);
+    cam.Render();
+    return cam.image;
+  };
+  const auto plain = render(0.0, false), zero = render(0.0, true), rolled = render(7.5, true);
+  CHECK(plain == zero);
+  CHECK(rolled != plain);
+  float mx = 0;
+  for (auto& row : rolled)
+    for (float v : row) mx = std::fmax(mx, v);
+  CHECK(mx > 0);
+}
+
 int main(int argc, char** argv) {
   std::string dir = argc > 1 ? argv[1] : ".";
   cmem_basic();
@@ -199,6 +231,7 @@ int main(int argc, char** argv) {
   datacube(dir);
   camera_files_and_accumulation(dir);
   concurrent_cameras();
+  camera_roll();
   std::printf("%d failures\n", failures);
   return failures;
 }
