@@ -369,12 +369,13 @@ def run_c4(args, B, O):
     n_cubes = args.c4_cubes
     t_setup = time.perf_counter()
     xs, ys, zs, bases = synth.serving_bases(nx, ny, nz)
-    layout = B.CUBE_COMPACT if args.c4_layout == "compact" else B.CUBE_RECORDS
-    records_share = int(args.c4_records_gb * (1 << 30)) if layout == B.CUBE_COMPACT else 0
+    codes = {"compact": B.CUBE_COMPACT, "pairs": B.CUBE_PAIRS, "records": B.CUBE_RECORDS}
+    layout, promoted = codes[args.c4_layout], codes[args.c4_promote_layout]
+    share = int(args.c4_promote_gb * (1 << 30)) if promoted != layout and layout != B.CUBE_RECORDS else 0
     srv = B.Server(B.server_config(cube_budget_bytes=int(args.c4_budget_gb * (1 << 30)), slots=3,
                                    max_batch_requests=64, max_batch_pixels=16 << 20, max_wait_ms=1.0,
-                                   max_queue=1 << 17, cube_layout=layout, records_budget_bytes=records_share,
-                                   uploaders=args.c4_uploaders))
+                                   max_queue=1 << 17, cube_layout=layout, promoted_layout=promoted,
+                                   promoted_budget_bytes=share, uploaders=args.c4_uploaders))
 
     def add(i):
         return srv.add_cube(xs, ys, zs, synth.serving_cube(i, bases))
@@ -503,24 +504,33 @@ def run_c4(args, B, O):
         pl.append(1000 * (time.perf_counter() - t))
     # the GPU's own rate on these requests: 256 of them batched on that one
     # resident cube (device time, L2 flushed), the ceiling a server can reach
-    its = [(cube, c) for c in cams[:256]]
-    cb = B.Batch(len(its), sum(c.nx * c.ny for _, c in its))
-    cb.render(its)
-    bms = []
-    for _ in range(3):
-        B.flush_l2()
-        cb.submit(its)
-        cb.wait()
-        bms.append(cb.last_ms()[0])
-    cb.close()
-    ceiling = len(its) / (min(bms) / 1000)
+    # (and the same in the promoted layout)
+    def batched_rate(c3d):
+        its = [(c3d, c) for c in cams[:256]]
+        cb = B.Batch(len(its), sum(c.nx * c.ny for _, c in its))
+        cb.render(its)
+        bms = []
+        for _ in range(3):
+            B.flush_l2()
+            cb.submit(its)
+            cb.wait()
+            bms.append(cb.last_ms()[0])
+        cb.close()
+        return len(its) / (min(bms) / 1000)
+
+    ceiling = batched_rate(cube)
     cube_bytes = cube.info().device_bytes
     cube.close()
+    ceiling_promoted = None
+    if share:
+        cube = B.Cube(xs, ys, zs, synth.serving_cube(0, bases), layout=promoted)
+        ceiling_promoted = batched_rate(cube)
+        cube.close()
     return {"workload": f"config 4 serving sweep: {n_cubes} cubes of {nx}x{ny}x{nz} FP32 "
                         f"({n_cubes * nx * ny * nz * 4 / 1e9:.1f} GB of pinned host copies), Zipf(1.1) popularity, "
                         f"{args.c4_budget_gb:g} GiB device budget, {args.c4_layout} layout"
-                        + (f" (up to {args.c4_records_gb:g} GiB of it for the most-requested cubes, promoted to "
-                           f"the records layout)" if records_share else "")
+                        + (f" (up to {args.c4_promote_gb:g} GiB of it for the most-requested cubes, promoted to "
+                           f"the {args.c4_promote_layout} layout)" if share else "")
                         + f", Poisson arrivals, {args.c4_seconds:g} s per offered rate (70% run: "
                           f"{2 * args.c4_seconds:g} s)",
             "cube_device_bytes": cube_bytes,
@@ -528,10 +538,12 @@ def run_c4(args, B, O):
             "setup_s": setup_s, "warm_s": warm_s, "warm_uploads": int(st_warm.cube_uploads),
             "sweep": sweep, "saturated": saturated, "saturation_images_s": sat,
             "gpu_batched_one_cube_images_s": ceiling,
+            "gpu_batched_one_cube_promoted_images_s": ceiling_promoted,
             "at_70pct_of_saturation": at70,
             "uploads_total": int(st_end.cube_uploads), "evictions_total": int(st_end.cube_evictions),
-            "records_share_gb": args.c4_records_gb if records_share else 0, "uploaders": args.c4_uploaders,
-            "promotions_to_records": int(st_end.cube_promotions), "records_bytes_end": int(st_end.records_bytes),
+            "promoted_share_gb": args.c4_promote_gb if share else 0,
+            "promoted_layout": args.c4_promote_layout if share else None, "uploaders": args.c4_uploaders,
+            "promotions": int(st_end.cube_promotions), "promoted_bytes_end": int(st_end.promoted_bytes),
             "plain": {"p50_ms": float(np.percentile(pl, 50)), "p99_ms": float(np.percentile(pl, 99)),
                       "images_s": len(pl) / (sum(pl) / 1000)},
             "parity": parity}
@@ -540,8 +552,8 @@ def run_c4(args, B, O):
 def run_profile_case(args):
     """A small fixed batch for profiling one kernel class: the first
     --requests requests of the orbit sampler on the 256^3 stretched cube
-    (trilinear or nearest, records or compact layout) or on the default CMEM
-    model, launched --launches times."""
+    (trilinear or nearest, records, pairs or compact layout) or on the
+    default CMEM model, launched --launches times."""
     import birp_cpp_gb300 as B
     from birp_cpp_gb300 import build, synth
     build.build()
@@ -552,7 +564,7 @@ def run_profile_case(args):
         space = B.Cmem()
     else:
         xs, ys, zs, v = synth.cube_config1(seed=1)
-        layout = B.CUBE_COMPACT if mode == "compact" else B.CUBE_RECORDS
+        layout = {"compact": B.CUBE_COMPACT, "pairs": B.CUBE_PAIRS}.get(mode, B.CUBE_RECORDS)
         space = B.Cube(xs, ys, zs, v.astype(np.float32), layout=layout)
     cams = [B.camera(p, a, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(s),
                      ray_length=synth.RAY_LENGTH, trilinear=mode != "nearest") for p, a, nx, ny, s in reqs]
@@ -683,7 +695,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4"],
                     help="c2: the default run (headline on config 2, plus the c3 and c4 blocks); c3 / c4: that "
                          "block alone")
-    ap.add_argument("--profile-case", choices=["trilinear", "nearest", "compact", "cmem"],
+    ap.add_argument("--profile-case", choices=["trilinear", "nearest", "compact", "pairs", "cmem"],
                     help="run a small fixed batch of one kernel class (for a profiler) and exit")
     ap.add_argument("--launches", type=int, default=4, help="launches of --profile-case")
     ap.add_argument("--c4-cubes", type=int, default=256)
@@ -691,11 +703,13 @@ def main():
     ap.add_argument("--c4-budget-gb", type=float, default=60.0)
     ap.add_argument("--c4-rates", default="50,200,500,1000,2000,3000,4000,6000,8000,12000,16000")
     ap.add_argument("--c4-seconds", type=float, default=4.0)
-    ap.add_argument("--c4-layout", default="compact", choices=["compact", "records"],
+    ap.add_argument("--c4-layout", default="compact", choices=["compact", "pairs", "records"],
                     help="device layout of the served cubes")
     ap.add_argument("--c4-uploaders", type=int, default=1, help="the server's parallel cube uploads")
-    ap.add_argument("--c4-records-gb", type=float, default=0.0,
-                    help="share of the budget for cubes the server promotes to the records layout (0: none)")
+    ap.add_argument("--c4-promote-layout", default="pairs", choices=["pairs", "records"],
+                    help="faster layout the server promotes its most-requested cubes to")
+    ap.add_argument("--c4-promote-gb", type=float, default=0.0,
+                    help="share of the budget for promoted cubes (0: no promotion)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if args.requests is None:

@@ -47,7 +47,7 @@ class Request(C.Structure):
     _fields_ = [("cube", C.c_void_p), ("cmem", C.c_void_p), ("cam", Camera)]
 
 
-CUBE_RECORDS, CUBE_COMPACT = 0, 1  # device layouts of a cube (birp_cube_create_layout)
+CUBE_RECORDS, CUBE_COMPACT, CUBE_PAIRS = 0, 1, 2  # device layouts of a cube (birp_cube_create_layout)
 
 
 class CubeInfo(C.Structure):
@@ -58,7 +58,8 @@ class CubeInfo(C.Structure):
 class ServerConfig(C.Structure):
     _fields_ = [("cube_budget_bytes", C.c_int64), ("slots", C.c_int), ("max_batch_requests", C.c_int),
                 ("max_batch_pixels", C.c_int64), ("max_queue", C.c_int), ("max_wait_ms", C.c_double),
-                ("cube_layout", C.c_int), ("records_budget_bytes", C.c_int64), ("uploaders", C.c_int)]
+                ("cube_layout", C.c_int), ("promoted_layout", C.c_int), ("promoted_budget_bytes", C.c_int64),
+                ("uploaders", C.c_int)]
 
 
 class Result(C.Structure):
@@ -69,7 +70,7 @@ class Result(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "completed", "rejected", "batches", "cube_uploads",
                                          "cube_evictions", "cube_hits", "resident_bytes", "cube_promotions",
-                                         "records_bytes")]
+                                         "promoted_bytes")]
 
 
 class KernelStats(C.Structure):
@@ -178,7 +179,8 @@ def camera_defaults() -> Camera:
 
 class Cube:
     """A DataCube resident in GPU memory (birp_cube_create_layout; layout
-    CUBE_RECORDS, the fastest, or CUBE_COMPACT, about 1/8 of the memory)."""
+    CUBE_RECORDS, the fastest, CUBE_PAIRS, about 1/4 of its memory, or
+    CUBE_COMPACT, about 1/8)."""
 
     def __init__(self, xs, ys, zs, values, layout: int = CUBE_RECORDS):
         xs = np.ascontiguousarray(xs, np.float64)

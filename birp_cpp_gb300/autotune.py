@@ -185,6 +185,7 @@ def write_table(plain, batch_tri, batch_near, batch_cmem, path):
 CLASSES = {  # class: (macro, candidates of resident CTAs per SM, profile case)
     "records": ("BIRP_WALK_MINB", [6, 7, 8], "trilinear"),
     "compact": ("BIRP_COMPACT_MINB", [5, 6, 7, 8], "compact"),
+    "pairs": ("BIRP_PAIRS_MINB", [6, 7, 8], "pairs"),
     "nearest": ("BIRP_NEAREST_MINB", [6, 7, 8], "nearest"),
     "cmem": ("BIRP_CMEM_MINB", [4, 5, 6, 7], "cmem"),
 }
@@ -210,7 +211,8 @@ if mode == "cmem":
     space = B.Cmem()
 else:
     xs, ys, zs, v = synth.cube_config1(seed=1)
-    space = B.Cube(xs, ys, zs, v.astype(np.float32), layout=B.CUBE_COMPACT if mode == "compact" else B.CUBE_RECORDS)
+    layout = {{"compact": B.CUBE_COMPACT, "pairs": B.CUBE_PAIRS}}.get(mode, B.CUBE_RECORDS)
+    space = B.Cube(xs, ys, zs, v.astype(np.float32), layout=layout)
 cams = [B.camera(p, a, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(s), trilinear=mode != "nearest")
         for p, a, nx, ny, s in reqs]
 items = [(space, c) for c in cams]

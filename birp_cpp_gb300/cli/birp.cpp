@@ -11,7 +11,7 @@
 //   -v -b -d -p -q -r -f -e -g -u -j -k -l   CMEM parameters as the reference
 //
 // Extensions (no reference counterpart):
-//   -m records|compact      device layout of the cubes (default records)
+//   -m records|pairs|compact device layout of the cubes (default records)
 //   -M n                    cubes rendered per GPU launch in batch mode (32)
 //
 // Batch mode differs from the reference in how it runs, not in what it
@@ -119,8 +119,9 @@ int main(int argc, char** argv) try {
       case 'l': density = std::stof(optarg); break;
       case 'm':
         if (std::string(optarg) == "compact") layout = BIRP_CUBE_COMPACT;
+        else if (std::string(optarg) == "pairs") layout = BIRP_CUBE_PAIRS;
         else if (std::string(optarg) == "records") layout = BIRP_CUBE_RECORDS;
-        else throw std::invalid_argument("-m takes records or compact");
+        else throw std::invalid_argument("-m takes records, pairs or compact");
         break;
       case 'M': per_launch = std::max(1, std::stoi(optarg)); break;
       default: return 1;

@@ -27,9 +27,10 @@ class DataCube : public Space {
   // Many samples in one GPU call; -1 outside the box.
   void GetSamples(const float* xyz, int n, float* out);
   void SetTrilinear(bool);
-  // Device layout of the GPU copy (BIRP_CUBE_RECORDS, the default, or
-  // BIRP_CUBE_COMPACT: ~1/8 of the memory, somewhat slower to render). No
-  // reference counterpart (the reference keeps the cube on the host).
+  // Device layout of the GPU copy (BIRP_CUBE_RECORDS, the default;
+  // BIRP_CUBE_PAIRS: ~1/4 of the memory, a little slower to render; or
+  // BIRP_CUBE_COMPACT: ~1/8 of the memory, slower). No reference counterpart
+  // (the reference keeps the cube on the host).
   void SetLayout(int layout);
   // Re-uploads the public fields after they were changed by the caller.
   void Upload();

@@ -254,7 +254,8 @@ void DataCube::Upload() {
 }
 
 void DataCube::SetLayout(int l) {
-  if (l != BIRP_CUBE_RECORDS && l != BIRP_CUBE_COMPACT) throw std::invalid_argument("unknown cube layout");
+  if (l != BIRP_CUBE_RECORDS && l != BIRP_CUBE_COMPACT && l != BIRP_CUBE_PAIRS)
+    throw std::invalid_argument("unknown cube layout");
   if (l != layout && gpu) {  // rebuilt on next use
     birp_cube_destroy(gpu);
     gpu = nullptr;

@@ -26,7 +26,9 @@ int request_class(const birp_request& r) {
   if (r.cmem) return BATCH_CMEM;
   if (!r.cam.trilinear) return BATCH_CUBE_NEAREST;
   if (r.cube && r.cube->has_neg > 0) return BATCH_CUBE_SIGNED;
-  return (r.cube && r.cube->layout == BIRP_CUBE_COMPACT) ? BATCH_CUBE_TRI_COMPACT : BATCH_CUBE_TRI;
+  if (r.cube && r.cube->layout == BIRP_CUBE_COMPACT) return BATCH_CUBE_TRI_COMPACT;
+  if (r.cube && r.cube->layout == BIRP_CUBE_PAIRS) return BATCH_CUBE_TRI_PAIRS;
+  return BATCH_CUBE_TRI;
 }
 
 static void free_batch(birp_batch* b) {
@@ -92,9 +94,10 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   std::memset(b->h_stage, 0, b->stage_bytes);
 
   // One graph: descriptors H2D, the queue heads reset, then the kernels of
-  // the five classes as parallel branches: CMEM (few but heavy requests),
-  // trilinear cubes holding negative values, nearest mode, and the two
-  // trilinear-cube kernels (compact and records layout). Each is a persistent kernel sized to fill the GPU on its own;
+  // the six classes as parallel branches: CMEM (few but heavy requests),
+  // trilinear cubes holding negative values, nearest mode, and the three
+  // trilinear-cube kernels (compact, pairs and records layout). Each is a
+  // persistent kernel sized to fill the GPU on its own;
   // launched side by side, the CTAs of one class take the SM slots that
   // another class's CTAs leave when its queue runs dry, so the classes of a
   // mixed batch overlap instead of each paying its tail in turn, and a class
@@ -116,7 +119,8 @@ birp_status batch_create(int max_requests, int64_t max_pixels, birp_batch** out)
   cudaMemcpyAsync(b->d_stage, b->h_stage, b->stage_bytes, cudaMemcpyHostToDevice, b->stream);
   cudaMemsetAsync(b->d_counter, 0, BATCH_CLASSES * sizeof(unsigned int), b->stream);
   cudaEventRecord(b->fork, b->stream);
-  for (int c : {BATCH_CMEM, BATCH_CUBE_SIGNED, BATCH_CUBE_NEAREST, BATCH_CUBE_TRI_COMPACT, BATCH_CUBE_TRI}) {
+  for (int c : {BATCH_CMEM, BATCH_CUBE_SIGNED, BATCH_CUBE_NEAREST, BATCH_CUBE_TRI_COMPACT, BATCH_CUBE_TRI_PAIRS,
+                BATCH_CUBE_TRI}) {
     cudaStreamWaitEvent(b->branch[c], b->fork, 0);
     launch_render_batch(bd[c], b->grid[c], b->branch[c], c);
     cudaEventRecord(b->join[c], b->branch[c]);

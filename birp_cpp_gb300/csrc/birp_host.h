@@ -24,7 +24,8 @@ struct birp_cube {
   float2* d_cells = nullptr;    // walk tables (up and down) of the 3 axes, concatenated
   int layout = BIRP_CUBE_RECORDS;
   float* d_grid = nullptr;      // compact layout: padded node values
-  float4* d_walk4 = nullptr;    // compact layout: walk tables with inverse widths
+  float2* d_pairs = nullptr;    // pairs layout: padded {value, z-slope} per node
+  float4* d_walk4 = nullptr;    // compact and pairs layouts: walk tables with inverse widths
   float2* d_nodes_ff = nullptr; // node coordinates as float pairs, 3 axes concatenated
   int has_neg = -1;             // a value below zero (-1: not yet known)
   uint8_t* d_negflag = nullptr; // its negative-value flags (CubeDev::negflag)

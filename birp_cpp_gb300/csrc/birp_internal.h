@@ -24,6 +24,12 @@
 //    about 1x the input), the march forming a cell's coefficients from its
 //    8 corners in FP32, and float4 walk tables {base, exit plane, 1/width, 0}
 //    (1/width = 0 at guard cells).
+//  * pairs layout (the middle ground: about 2x the input, near the records
+//    layout's speed): the same padded grid, each node a float2 {v, s} of its
+//    value and the slope of its z-edge, s = (v(k+1) - v(k)) / (z(k+1) - z(k))
+//    computed in FP64 (0 on the guard cells along z), so a cell's 4 z-edges
+//    {c + s z} are 4 8-byte loads whose differences along x and y give its 8
+//    coefficients; float4 walk tables as in the compact layout.
 //  * per-axis index tables (LUT) for nonuniform axes: float4 bins of width at
 //    most the smallest cell, each holding one piecewise-linear index map.
 //  * FP64 axis coordinates, read only by the exact (FP64) decisions.
@@ -65,9 +71,12 @@ struct CubeDev {
   // FP64 coordinate to ~48 bits), for the nearest-mode crossings; entries
   // -1 and n are the sentinels -inf and +inf
   const float2* nodes_ff[3];
-  // compact layout (rec == nullptr): padded node values and their strides,
-  // and the float4 walk tables (same indexing as walk_up / walk_dn)
-  int compact;
+  // compact and pairs layouts (rec == nullptr): padded node values and their
+  // strides, and the float4 walk tables (same indexing as walk_up / walk_dn).
+  // Node (i, j, k)'s value is grid[record_index(gx, gxy, i, j, k) << gshift]
+  // (gshift 0: compact, one float per node; 1: pairs, {v, s} per node).
+  int node_vals;        // 1 in the compact and pairs layouts
+  int gshift;
   const float* grid;
   uint32_t gx;          // nx + 2
   uint32_t gxy;         // (nx + 2) * (ny + 2)
@@ -110,6 +119,8 @@ struct CmemParam {
 };
 
 enum SpaceKind : int { SPACE_CUBE = 0, SPACE_CMEM = 1 };
+// Device layouts of a cube (the values of BIRP_CUBE_*).
+enum CubeLayout : int { CUBE_RECORDS = 0, CUBE_COMPACT = 1, CUBE_PAIRS = 2 };
 enum MarchMode : int { MARCH_PREFIX = 0, MARCH_CLIP = 1 };
 
 // One render request as the kernels see it (per camera).
@@ -135,7 +146,7 @@ struct RequestDev {
   int wgx_l2;        // 2^wgx_l2 of the CTA's 4 warps sit across the tile
   int tiles_x;       // tiles along x for this request's tile shape
   int tiles;         // total tiles
-  int compact;       // cube: 1 in the compact layout (node values, no records)
+  int layout;        // cube: CUBE_RECORDS, CUBE_COMPACT or CUBE_PAIRS
   int has_neg;       // cube: 1 when it holds a value below zero (it carries flags)
   const CubeDev* cube;   // device pointer (kind == SPACE_CUBE)
   const CmemDev* cmem;   // device pointer (kind == SPACE_CMEM)
@@ -173,9 +184,9 @@ cudaError_t launch_render_plain(const RequestDev& req, KernelStats* stats, cudaS
                                 const CmemDev* cmem_host = nullptr);
 // Persistent-kernel classes: trilinear cube requests in the records layout
 // (fewer registers, more resident warps than the general kernel), the same in
-// the compact layout, CMEM requests, nearest-mode cube requests (either
-// layout), trilinear requests of cubes holding a negative value (either
-// layout; FP64 sums next to negative nodes), and the general kernel that
+// the compact and in the pairs layout, CMEM requests, nearest-mode cube
+// requests (any layout), trilinear requests of cubes holding a negative value
+// (any layout; FP64 sums next to negative nodes), and the general kernel that
 // renders any request (used where one launch must take a mix, see
 // birp_batch_render_noalloc).
 enum BatchClass : int {
@@ -184,8 +195,9 @@ enum BatchClass : int {
   BATCH_CUBE_TRI_COMPACT = 2,
   BATCH_CMEM = 3,
   BATCH_CUBE_NEAREST = 4,
-  BATCH_CUBE_SIGNED = 5,  // trilinear cubes holding a negative value, either layout
-  BATCH_CLASSES = 6
+  BATCH_CUBE_SIGNED = 5,  // trilinear cubes holding a negative value, any layout
+  BATCH_CUBE_TRI_PAIRS = 6,
+  BATCH_CLASSES = 7
 };
 // model: the CMEM model the CMEM class kernel takes as a parameter (nullptr:
 // none, every request reads its model through its pointer)
@@ -205,6 +217,10 @@ cudaError_t launch_cube_negflags(const float* padded, int nx, int ny, int nz, ui
 bool read_bounds_status(unsigned long long* status, bool reset);
 cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, const double* cx64, const double* cy64,
                                 const double* cz64, float4* rec, cudaStream_t stream);
+// the pairs layout's {value, z-slope} per padded node (padded: the guard-filled
+// scalar grid; cz64: the FP64 z coordinates)
+cudaError_t launch_cube_pairs(const float* padded, int nx, int ny, int nz, const double* cz64, float2* pairs,
+                              cudaStream_t stream);
 cudaError_t launch_cube_sample(const CubeDev* cube, int trilinear, const float* xyz, int n, float* out,
                                cudaStream_t stream);
 cudaError_t launch_cmem_sample(const CmemDev* cmem, const float* xyz, int n, float* out, cudaStream_t stream);

@@ -248,7 +248,7 @@ birp_status build_request(const birp_cube* cube, const birp_cmem* cmem, const bi
   r.out = out;
   if (cube) {
     r.cube = cube->d_desc;
-    r.compact = cube->h_desc.compact;
+    r.layout = cube->layout;
     r.has_neg = cube->has_neg > 0 ? 1 : 0;
   } else {
     r.cmem = cmem->d_desc;
@@ -393,6 +393,9 @@ void birp_shutdown(void) {
 
 // ---------------------------------------------------------------- cube
 
+static_assert(BIRP_CUBE_RECORDS == CUBE_RECORDS && BIRP_CUBE_COMPACT == CUBE_COMPACT && BIRP_CUBE_PAIRS == CUBE_PAIRS,
+              "the kernels' layout codes are the ABI's");
+
 birp_status birp_cube_create(const double* xs, int nx, const double* ys, int ny, const double* zs, int nz,
                              const float* values, birp_cube** out) {
   return birp_cube_create_layout(xs, nx, ys, ny, zs, nz, values, BIRP_CUBE_RECORDS, out);
@@ -402,7 +405,7 @@ birp_status birp_cube_create_layout(const double* xs, int nx, const double* ys, 
                                     const float* values, int layout, birp_cube** out) {
   if (birp_status s = check_init()) return s;
   if (!out || !values || !xs || !ys || !zs) return fail(BIRP_ERR_INVALID, "NULL argument");
-  if (layout != BIRP_CUBE_RECORDS && layout != BIRP_CUBE_COMPACT)
+  if (layout != BIRP_CUBE_RECORDS && layout != BIRP_CUBE_COMPACT && layout != BIRP_CUBE_PAIRS)
     return fail(BIRP_ERR_INVALID, "unknown cube layout %d", layout);
   *out = nullptr;
   const double* axes[3] = {xs, ys, zs};

@@ -102,13 +102,14 @@ void destroy_cube_device(birp_cube& c) {
   if (c.alloc_stream) {
     // stream-ordered pool memory: no device-wide synchronisation on release
     for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
-                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff, (void*)c.d_negflag})
+                    (void*)c.d_grid, (void*)c.d_pairs, (void*)c.d_walk4, (void*)c.d_nodes_ff, (void*)c.d_negflag})
       if (p) cudaFreeAsync(p, c.alloc_stream);
   } else {
     for (void* p : {(void*)c.d_vals, (void*)c.d_c64, (void*)c.d_lut, (void*)c.d_desc, (void*)c.d_cells,
-                    (void*)c.d_grid, (void*)c.d_walk4, (void*)c.d_nodes_ff, (void*)c.d_negflag})
+                    (void*)c.d_grid, (void*)c.d_pairs, (void*)c.d_walk4, (void*)c.d_nodes_ff, (void*)c.d_negflag})
       if (p) cudaFree(p);
   }
+  c.d_pairs = nullptr;
   c.d_negflag = nullptr;
   c.d_nodes_ff = nullptr;
   c.d_grid = nullptr;
@@ -164,11 +165,13 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   // then the down table in reverse cell order. Guard cells take the edge node
   // as base (their coefficients along the axis are 0) and an infinite exit
   // plane, so the walk stops there. Records layout: float2 {base, exit
-  // plane}; compact layout: float4 {base, exit plane, 1/width (0 at guard
-  // cells), 0}. One padding entry at the end: a walk that reads one entry
-  // ahead of its cell may read one past the last table's guard cell (the
-  // value is never used).
+  // plane}; compact and pairs layouts: float4 {base, exit plane, 1/width (0
+  // at guard cells), 0}. One padding entry at the end: a walk that reads one
+  // entry ahead of its cell may read one past the last table's guard cell
+  // (the value is never used).
   const bool compact = c.layout == BIRP_CUBE_COMPACT;
+  const bool pairs = c.layout == BIRP_CUBE_PAIRS;
+  const bool nodes_layout = compact || pairs;  // node values (no records)
   std::vector<float4> walk;
   walk.reserve(2 * (coords + 3) + 1);
   size_t up_off[3], dn_off[3];
@@ -187,18 +190,20 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   }
   walk.push_back(make_float4(0.f, 0.f, 0.f, 0.f));
   std::vector<float2> walk2;
-  if (!compact) {
+  if (!nodes_layout) {
     walk2.reserve(walk.size());
     for (const float4& w : walk) walk2.push_back(make_float2(w.x, w.y));
   }
   const size_t records = ((size_t)nx + 1) * ((size_t)ny + 1) * ((size_t)nz + 1);
-  // the padded scalar grid; records layout: turned into records, then freed
-  // (held in d_grid until then, so a failed upload releases it with the rest)
+  // the padded scalar grid; records and pairs layouts: turned into records
+  // (pairs), then freed (held in d_grid until then, so a failed upload
+  // releases it with the rest)
   float* scalar = nullptr;
   CKU(dev_alloc(&scalar, total * sizeof(float), c.alloc_stream));
   c.d_grid = scalar;
-  if (compact) {
+  if (nodes_layout) {
     CKU(dev_alloc(&c.d_walk4, walk.size() * sizeof(float4), c.alloc_stream));
+    if (pairs) CKU(dev_alloc(&c.d_pairs, total * sizeof(float2), c.alloc_stream));
   } else {
     CKU(dev_alloc(&c.d_cells, walk2.size() * sizeof(float2), c.alloc_stream));
     CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
@@ -211,6 +216,7 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   c.device_bytes = coords * sizeof(double) + (coords + 6) * sizeof(float2) + lut.size() * sizeof(float4) +
                    sizeof(CubeDev) + (c.has_neg ? nodes : 0) +
                    (compact ? total * sizeof(float) + walk.size() * sizeof(float4)
+                    : pairs ? total * sizeof(float2) + walk.size() * sizeof(float4)
                             : records * 2 * sizeof(float4) + walk2.size() * sizeof(float2));
 
   // interior values from the caller's x-fastest array: pinned host memory
@@ -254,8 +260,15 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     nodes_ff.push_back(make_float2(INFINITY, 0.f));
   }
   CKU(cudaMemcpyAsync(c.d_nodes_ff, nodes_ff.data(), nodes_ff.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
-  if (compact) {
+  if (nodes_layout) {
     CKU(cudaMemcpyAsync(c.d_walk4, walk.data(), walk.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+    if (pairs) {
+      CKU(launch_cube_pairs(scalar, nx, ny, nz, c.d_c64 + nx + ny, c.d_pairs, st));
+      if (c.alloc_stream) {
+        c.d_grid = nullptr;
+        CKU(cudaFreeAsync(scalar, st));
+      }
+    }
   } else {
     CKU(launch_cube_records(scalar, nx, ny, nz, c.d_c64, c.d_c64 + nx, c.d_c64 + nx + ny, c.d_vals, st));
     if (c.alloc_stream) {
@@ -285,8 +298,8 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
     off += a.n;
   }
   d.negflag = c.d_negflag;
-  d.rec_f4 = compact ? 0 : (long long)(records * 2);
-  d.grid_n = compact ? (long long)total : 0;
+  d.rec_f4 = nodes_layout ? 0 : (long long)(records * 2);
+  d.grid_n = compact ? (long long)total : pairs ? 2 * (long long)total : 0;
   d.walk_n = (int)walk.size();
   d.nodes_n = (int)nodes_ff.size();
   d.lut_total = (int)lut.size();
@@ -305,12 +318,13 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   d.cx = (uint32_t)(nx + 1);
   d.cxy = (uint32_t)((nx + 1) * (ny + 1));
   d.lut = c.d_lut;
-  d.compact = compact ? 1 : 0;
-  d.grid = compact ? c.d_grid : nullptr;
+  d.node_vals = nodes_layout ? 1 : 0;
+  d.gshift = pairs ? 1 : 0;
+  d.grid = compact ? c.d_grid : pairs ? reinterpret_cast<const float*>(c.d_pairs) : nullptr;
   d.gx = (uint32_t)px;
   d.gxy = (uint32_t)(px * py);
   for (int k = 0; k < 3; ++k) {
-    if (compact) {
+    if (nodes_layout) {
       d.walk4_up[k] = c.d_walk4 + up_off[k];
       d.walk4_dn[k] = c.d_walk4 + dn_off[k];
     } else {
@@ -341,9 +355,10 @@ size_t cube_device_bytes(const birp_cube& c) {
   const size_t walk = 2 * (coords + 3) + 1;
   const size_t records = ((size_t)c.n[0] + 1) * ((size_t)c.n[1] + 1) * ((size_t)c.n[2] + 1);
   const size_t nodes_ff = (coords + 6) * sizeof(float2);
-  const size_t layout_bytes = nodes_ff + (c.layout == BIRP_CUBE_COMPACT
-                                              ? total * sizeof(float) + walk * sizeof(float4)
-                                              : records * 2 * sizeof(float4) + walk * sizeof(float2));
+  const size_t layout_bytes =
+      nodes_ff + (c.layout == BIRP_CUBE_COMPACT ? total * sizeof(float) + walk * sizeof(float4)
+                  : c.layout == BIRP_CUBE_PAIRS ? total * sizeof(float2) + walk * sizeof(float4)
+                                                : records * 2 * sizeof(float4) + walk * sizeof(float2));
   const size_t negflag = c.has_neg > 0 ? (size_t)c.n[0] * c.n[1] * c.n[2] : 0;
   return layout_bytes + coords * sizeof(double) + lut + sizeof(CubeDev) + negflag;
 }

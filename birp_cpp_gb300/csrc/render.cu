@@ -43,6 +43,9 @@ constexpr int kThreads = 128;
 #ifndef BIRP_COMPACT_MINB
 #define BIRP_COMPACT_MINB BIRP_COMPACT_MINB_TUNED  // compact-layout trilinear (forms 8 corners per cell)
 #endif
+#ifndef BIRP_PAIRS_MINB
+#define BIRP_PAIRS_MINB BIRP_PAIRS_MINB_TUNED  // pairs-layout trilinear (4 z-edges per cell)
+#endif
 #ifndef BIRP_NEAREST_MINB
 #define BIRP_NEAREST_MINB BIRP_NEAREST_MINB_TUNED  // nearest mode
 #endif
@@ -50,7 +53,7 @@ constexpr int kThreads = 128;
 #define BIRP_CMEM_MINB BIRP_CMEM_MINB_TUNED  // CMEM
 #endif
 #ifndef BIRP_SIGNED_MINB
-#define BIRP_SIGNED_MINB 4  // trilinear cubes holding negative values (either layout, FP64 cell sums)
+#define BIRP_SIGNED_MINB 4  // trilinear cubes holding negative values (any layout, FP64 cell sums)
 #endif
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
@@ -525,16 +528,17 @@ __device__ __forceinline__ double lerp64(double a, double b, double t) {
   return ((t > 1.0) == (b > a)) ? (b < x ? x : b) : (b > x ? x : b);
 }
 
-// Node (i, j, k)'s input value in either layout: the padded grid, or c0 of
-// the record of the cell whose lower corner it is (exactly the FP32 input).
+// Node (i, j, k)'s input value in any layout: the padded grid (one float or
+// the first of a pair per node), or c0 of the record of the cell whose lower
+// corner it is (exactly the FP32 input).
 __device__ __forceinline__ double node_value(const CubeDev& C, int i, int j, int k) {
 #ifdef BIRP_DEBUG_BOUNDS
-  long long o = C.compact ? record_index(C.gx, C.gxy, i, j, k) : 8 * record_index(C.cx, C.cxy, i, j, k);
-  if (!bound_ok(o, C.compact ? C.grid_n : 4 * C.rec_f4, 2)) o = 0;
-  return C.compact ? (double)__ldg(C.grid + o) : (double)__ldg(reinterpret_cast<const float*>(C.rec) + o);
+  long long o = C.node_vals ? record_index(C.gx, C.gxy, i, j, k) << C.gshift : 8 * record_index(C.cx, C.cxy, i, j, k);
+  if (!bound_ok(o, C.node_vals ? C.grid_n : 4 * C.rec_f4, 2)) o = 0;
+  return C.node_vals ? (double)__ldg(C.grid + o) : (double)__ldg(reinterpret_cast<const float*>(C.rec) + o);
 #else
-  return C.compact ? (double)__ldg(C.grid + record_index(C.gx, C.gxy, i, j, k))
-                   : (double)__ldg(reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, i, j, k));
+  return C.node_vals ? (double)__ldg(C.grid + (record_index(C.gx, C.gxy, i, j, k) << C.gshift))
+                     : (double)__ldg(reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, i, j, k));
 #endif
 }
 
@@ -649,9 +653,11 @@ __device__ __forceinline__ int neg_search(const RequestDev* Rp, float d0, float 
 
 enum Interp { NEAREST = 0, TRILINEAR = 1 };
 // Cube layout of the march: cubes are walked cell by cell along the ray
-// (AXES_DDA over the records layout, AXES_DDA_COMPACT over the compact layout;
-// trilinear and nearest). CMEM requests carry AXES_NONE.
-enum Axes { AXES_NONE = 0, AXES_DDA = 2, AXES_DDA_COMPACT = 3 };
+// (AXES_DDA over the records layout, AXES_DDA_COMPACT over the compact layout
+// and, in nearest mode, over the pairs layout too (node values at a stride),
+// AXES_DDA_PAIRS the trilinear walk over the pairs layout). CMEM requests
+// carry AXES_NONE.
+enum Axes { AXES_NONE = 0, AXES_DDA = 2, AXES_DDA_COMPACT = 3, AXES_DDA_PAIRS = 4 };
 
 // One pixel tile of one request. The lanes-per-ray split S = 2^seg_log2 is a
 // runtime value of the request (it only sets the tile shape, the lane -> ray
@@ -883,8 +889,11 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 
   int nsamp = iters;  // samples this lane evaluates (for the counters)
   if constexpr (KIND == SPACE_CUBE && INTERP == TRILINEAR) {
-    static_assert(AXES == AXES_DDA || AXES == AXES_DDA_COMPACT, "cubes march with AXES_DDA[_COMPACT]");
+    static_assert(AXES == AXES_DDA || AXES == AXES_DDA_COMPACT || AXES == AXES_DDA_PAIRS,
+                  "cubes march with AXES_DDA[_COMPACT|_PAIRS]");
     constexpr bool COMPACT = AXES == AXES_DDA_COMPACT;
+    constexpr bool PAIRS = AXES == AXES_DDA_PAIRS;
+    constexpr bool NODES = COMPACT || PAIRS;  // node-value layouts: float4 walk entries with 1/width
     // Cell-space integration. A lane takes a contiguous run of its ray's
     // samples and walks the cells the run crosses. Per axis the sample
     // position relative to the current cell's base node is affine in the
@@ -911,16 +920,17 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     // per axis: position step st, its reciprocal, position at the run's first
     // sample, the run's first position relative to the current cell's base
     // node (xb), the exit index ex (= plane * rst + nb, nb = -bs * rst: one
-    // FMA per step), the walk-table pointer and the record step (compact
-    // layout: the inverse width iw of the current cell and the pointer g to
-    // its lower corner node instead of the record pointer q)
-    using WalkEntry = std::conditional_t<COMPACT, float4, float2>;
+    // FMA per step), the walk-table pointer and the record step (compact and
+    // pairs layouts: the inverse width iw of the current cell and the pointer
+    // g (gp) to its lower corner node (z-edge) instead of the record pointer q)
+    using WalkEntry = std::conditional_t<NODES, float4, float2>;
     float st[3], rst[3], bs[3], xb[3], ex[3], nb[3];
     [[maybe_unused]] float iw[3];
     const WalkEntry* wt[3];
     int dstr[3];
     const float4* q = C.rec;
     [[maybe_unused]] const float* g = C.grid;
+    [[maybe_unused]] const float2* gp = reinterpret_cast<const float2*>(C.grid);
     if (count > 0) {
       const float f0 = (float)first_c;
       int k0s[3];
@@ -937,11 +947,11 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         // direction from the sign bit: a zero step of either sign (rst =
         // +-inf) then gives an exit index of +inf (or NaN), never a crossing
         const bool up = !signbit(d32[k]);
-        if constexpr (COMPACT) wt[k] = up ? C.walk4_up[k] + k0s[k] : C.walk4_dn[k] - k0s[k];
+        if constexpr (NODES) wt[k] = up ? C.walk4_up[k] + k0s[k] : C.walk4_dn[k] - k0s[k];
         else wt[k] = up ? C.walk_up[k] + k0s[k] : C.walk_dn[k] - k0s[k];
 #ifdef BIRP_DEBUG_BOUNDS
         {
-          const WalkEntry* wb = (COMPACT ? (const WalkEntry*)C.walk4_up[0] : (const WalkEntry*)C.walk_up[0]) - 1;
+          const WalkEntry* wb = (NODES ? (const WalkEntry*)C.walk4_up[0] : (const WalkEntry*)C.walk_up[0]) - 1;
           if (!bound_ok(wt[k] - wb, C.walk_n, 5)) wt[k] = wb;
         }
 #endif
@@ -950,7 +960,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         // exit index of the cell along this axis: bs + ex * st = exit plane
         nb[k] = -bs[k] * rst[k];
         ex[k] = fmaf(e.y, rst[k], nb[k]);
-        if constexpr (COMPACT) {
+        if constexpr (NODES) {
           iw[k] = e.z;
           const int stride = (int)record_stride(C.gx, C.gxy, k);  // in nodes
           dstr[k] = up ? stride : -stride;
@@ -960,6 +970,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         }
       }
       if constexpr (COMPACT) g = C.grid + record_index(C.gx, C.gxy, k0s[0], k0s[1], k0s[2]);
+      else if constexpr (PAIRS) gp += record_index(C.gx, C.gxy, k0s[0], k0s[1], k0s[2]);
       else q = C.rec + 2 * record_index(C.cx, C.cxy, k0s[0], k0s[1], k0s[2]);
       [[maybe_unused]] const int gx = (int)C.gx, gxy = (int)C.gxy;
       // the ray's step products, the same in every cell (local coordinates
@@ -989,6 +1000,24 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           const float ixy = iw[0] * iw[1];
           lo = make_float4(v000, d3 * iw[2], d1 * iw[0], e5 * (iw[0] * iw[2]));
           hi = make_float4(d2 * iw[1], e6 * (iw[1] * iw[2]), e4 * ixy, e7 * (ixy * iw[2]));
+        } else if constexpr (PAIRS) {
+          // the cell's 4 z-edges {c + s z} at its (x, y) corners; their
+          // differences along x and y (scaled by the inverse widths) are the
+          // coefficient pairs {c1, c5}, {c2, c6}, {c4, c7}. Scalar operations:
+          // as packed FP32x2 ones they all take the heavy FMA pipe, which
+          // the cell sum's packed FMAs already keep busy (9.39 ms against
+          // 9.12 ms on 64 orbit renders of the 256^3 cube)
+#ifdef BIRP_DEBUG_BOUNDS
+          if (!bound_ok(gp - reinterpret_cast<const float2*>(C.grid), (C.grid_n >> 1) - (gx + 1), 7))
+            gp = reinterpret_cast<const float2*>(C.grid);
+#endif
+          const float2 e00 = __ldg(gp), e10 = __ldg(gp + 1), e01 = __ldg(gp + gx), e11 = __ldg(gp + gx + 1);
+          const float dxa = e10.x - e00.x, dxb = e10.y - e00.y;
+          const float dya = e01.x - e00.x, dyb = e01.y - e00.y;
+          const float dxya = (e11.x - e01.x) - dxa, dxyb = (e11.y - e01.y) - dxb;
+          const float ixy = iw[0] * iw[1];
+          lo = make_float4(e00.x, e00.y, dxa * iw[0], dxb * iw[0]);
+          hi = make_float4(dya * iw[1], dyb * iw[1], dxya * ixy, dxyb * ixy);
         } else {
 #ifdef BIRP_DEBUG_BOUNDS
           if (!bound_ok(q - C.rec, C.rec_f4 - 1, 6)) q = C.rec;
@@ -1007,7 +1036,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
               long long j;
-              if constexpr (COMPACT) j = signbit(d32[k]) ? C.walk4_dn[k] - wt[k] : wt[k] - C.walk4_up[k];
+              if constexpr (NODES) j = signbit(d32[k]) ? C.walk4_dn[k] - wt[k] : wt[k] - C.walk4_up[k];
               else j = signbit(d32[k]) ? C.walk_dn[k] - wt[k] : wt[k] - C.walk_up[k];
               cj[k] = (int)min(max(j, 0ll), (long long)C.ax[k].n - 2);
             }
@@ -1069,7 +1098,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
             ++wt[k];
 #ifdef BIRP_DEBUG_BOUNDS
             {
-              const WalkEntry* wb = (COMPACT ? (const WalkEntry*)C.walk4_up[0] : (const WalkEntry*)C.walk_up[0]) - 1;
+              const WalkEntry* wb = (NODES ? (const WalkEntry*)C.walk4_up[0] : (const WalkEntry*)C.walk_up[0]) - 1;
               if (!bound_ok(wt[k] - wb, C.walk_n, 5)) wt[k] = wb;
             }
 #endif
@@ -1079,6 +1108,9 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
             if constexpr (COMPACT) {
               iw[k] = e.z;
               g += dstr[k];
+            } else if constexpr (PAIRS) {
+              iw[k] = e.z;
+              gp += dstr[k];
             } else {
               q += dstr[k];
             }
@@ -1099,7 +1131,7 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     // bound E; when u is within E of an integer the oracle's FP64 predicate
     // decides (a bracketed search over pos64). The lane's first cell is
     // located the same way. All counts are exact integers.
-    constexpr bool COMPACT = AXES == AXES_DDA_COMPACT;
+    constexpr bool COMPACT = AXES == AXES_DDA_COMPACT;  // node values (compact or pairs layout)
     const CubeDev& C = *R.cube;
     const int total = b - a;
     const int seglen = (total + S - 1) >> SEGL2;
@@ -1248,13 +1280,14 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
         }
         kc[k] = kk;
         nxtc[k] = cross(k, np[k]) - first_c;
-        const int stride = COMPACT ? (int)record_stride(C.gx, C.gxy, k) : 8 * (int)record_stride(C.cx, C.cxy, k);
+        const int stride =
+            COMPACT ? (int)record_stride(C.gx, C.gxy, k) << C.gshift : 8 * (int)record_stride(C.cx, C.cxy, k);
         dstr[k] = up ? stride : -stride;  // in floats
       }
-      // node value pointer: the padded grid (compact) or the first float of
-      // the cell's record (8 floats); cells stay within [-1, n-1], whose data
-      // exist, because a walk stops at the sentinel planes
-      const float* q = COMPACT ? C.grid + record_index(C.gx, C.gxy, kc[0], kc[1], kc[2])
+      // node value pointer: the padded grid (compact, pairs) or the first
+      // float of the cell's record (8 floats); cells stay within [-1, n-1],
+      // whose data exist, because a walk stops at the sentinel planes
+      const float* q = COMPACT ? C.grid + (record_index(C.gx, C.gxy, kc[0], kc[1], kc[2]) << C.gshift)
                                : reinterpret_cast<const float*>(C.rec) + 8 * record_index(C.cx, C.cxy, kc[0], kc[1], kc[2]);
       // the next planes as indices into the node table of all three axes
       // (one allocation: axis k's nodes start at nodes_ff[k])
@@ -1423,12 +1456,14 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
   if (R.kind == SPACE_CMEM) {
     render_tile<SPACE_CMEM, TRILINEAR, AXES_NONE>(R, tx, ty, sm, st);
   } else if (R.interp && R.has_neg) {
-    if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true>(R, tx, ty, sm, st);
+    if (R.layout == CUBE_COMPACT) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true>(R, tx, ty, sm, st);
+    else if (R.layout == CUBE_PAIRS) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_PAIRS, true>(R, tx, ty, sm, st);
     else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA, true>(R, tx, ty, sm, st);
   } else if (R.interp) {
-    if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
+    if (R.layout == CUBE_COMPACT) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
+    else if (R.layout == CUBE_PAIRS) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_PAIRS>(R, tx, ty, sm, st);
     else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, st);
-  } else if (R.compact) {
+  } else if (R.layout != CUBE_RECORDS) {
     render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, st);
   } else {
     render_tile<SPACE_CUBE, NEAREST, AXES_DDA>(R, tx, ty, sm, st);
@@ -1440,7 +1475,7 @@ __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& s
 // queue is empty. Items are numbered in the host's order (largest work
 // first). CLS = BATCH_CUBE_TRI compiles only the trilinear cube march (fewer
 // registers, more resident warps); BATCH_CUBE_SIGNED the trilinear march of
-// cubes holding negative values (either layout); BATCH_ANY renders every
+// cubes holding negative values (any layout); BATCH_ANY renders every
 // request kind.
 // `model`: the CMEM class kernel reads this CMEM model's constants as
 // parameter operands for the requests that use it (model.dev).
@@ -1449,6 +1484,7 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
                                            : CLS == BATCH_CMEM         ? BIRP_CMEM_MINB
                                            : CLS == BATCH_CUBE_NEAREST ? BIRP_NEAREST_MINB
                                            : CLS == BATCH_CUBE_TRI_COMPACT ? BIRP_COMPACT_MINB
+                                           : CLS == BATCH_CUBE_TRI_PAIRS ? BIRP_PAIRS_MINB
                                            : CLS == BATCH_CUBE_SIGNED  ? BIRP_SIGNED_MINB
                                                                        : BIRP_WALK_MINB)
     render_batch_kernel(BatchDev B, const __grid_constant__ CmemParam model) {
@@ -1476,13 +1512,16 @@ __global__ void __launch_bounds__(kThreads, CLS == BATCH_ANY          ? 1
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CUBE_TRI_COMPACT) {
       render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
+    } else if constexpr (CLS == BATCH_CUBE_TRI_PAIRS) {
+      render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_PAIRS>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CMEM) {
       render_tile<SPACE_CMEM, TRILINEAR, AXES_NONE>(R, tx, ty, sm, B.stats, &model);
     } else if constexpr (CLS == BATCH_CUBE_NEAREST) {
-      if (R.compact) render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
+      if (R.layout != CUBE_RECORDS) render_tile<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT>(R, tx, ty, sm, B.stats);
       else render_tile<SPACE_CUBE, NEAREST, AXES_DDA>(R, tx, ty, sm, B.stats);
     } else if constexpr (CLS == BATCH_CUBE_SIGNED) {
-      if (R.compact) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true>(R, tx, ty, sm, B.stats);
+      if (R.layout == CUBE_COMPACT) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true>(R, tx, ty, sm, B.stats);
+      else if (R.layout == CUBE_PAIRS) render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA_PAIRS, true>(R, tx, ty, sm, B.stats);
       else render_tile<SPACE_CUBE, TRILINEAR, AXES_DDA, true>(R, tx, ty, sm, B.stats);
     } else {
       render_tile_any(R, tx, ty, sm, B.stats);
@@ -1568,6 +1607,21 @@ __global__ void cube_records_kernel(const float* __restrict__ v, int nx, int ny,
   }
 }
 
+// Pairs layout from the padded scalar grid: every padded node (i, j, k) gets
+// {v, s}, s the slope of its z-edge (v(k+1) - v(k)) / (z(k+1) - z(k)) in FP64
+// rounded once (the records layout's c3 of the cell above it, bit for bit),
+// 0 where that cell is a guard cell (its values repeat the edge node).
+__global__ void cube_pairs_kernel(const float* __restrict__ v, int nx, int ny, int nz, const double* __restrict__ cz64,
+                                  float2* __restrict__ pairs) {
+  const long long pxy = (long long)(nx + 2) * (ny + 2);
+  const long long n = pxy * (nz + 2);
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const double iz = inv_width(cz64, nz, t / pxy);  // 0 unless the padded layer is 1..nz-1
+    const float v0 = v[t];
+    pairs[t] = make_float2(v0, iz != 0.0 ? (float)(((double)v[t + pxy] - (double)v0) * iz) : 0.f);
+  }
+}
+
 // Negative-value flags (CubeDev::negflag) from the padded scalar grid: node
 // (i, j, k) is flagged when a node of [i-1, i+2] x [j-1, j+2] x [k-1, k+2],
 // clamped to the grid, is below zero.
@@ -1615,16 +1669,19 @@ __global__ void cube_sample_kernel(const CubeDev* __restrict__ cube, int triline
       out[t] = -1.f;
       continue;
     }
-    if (C.compact) {
-      // FP64 lerps x -> y -> z of the 8 corner nodes
-      const float* g = C.grid + record_index(C.gx, C.gxy, k[0], k[1], k[2]);
+    if (C.node_vals) {
+      // FP64 lerps x -> y -> z of the 8 corner nodes (values at a stride of
+      // 2^gshift floats)
+      const int sh = C.gshift;
+      const float* g = C.grid + (record_index(C.gx, C.gxy, k[0], k[1], k[2]) << sh);
       const long long gx = C.gx, gxy = C.gxy;
       if (!trilinear) {
         out[t] = g[0];
         continue;
       }
       const double fx = f[0] / w[0], fy = f[1] / w[1], fz = f[2] / w[2];
-      auto lx = [&](long long o) { return (double)g[o] + fx * ((double)g[o + 1] - (double)g[o]); };
+      auto nv = [&](long long o) { return (double)g[o << sh]; };
+      auto lx = [&](long long o) { return nv(o) + fx * (nv(o + 1) - nv(o)); };
       const double y0 = lx(0) + fy * (lx(gx) - lx(0));
       const double y1 = lx(gxy) + fy * (lx(gxy + gx) - lx(gxy));
       out[t] = (float)(y0 + fz * (y1 - y0));
@@ -1785,14 +1842,19 @@ cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStr
     cp.dev = h.cmem;
   }
   if (h.kind == SPACE_CMEM) render_plain_kernel<SPACE_CMEM, TRILINEAR, AXES_NONE><<<grid, kThreads, 0, s>>>(h, cp, stats);
-  else if (h.interp && h.has_neg && h.compact)
+  else if (h.interp && h.has_neg && h.layout == CUBE_COMPACT)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT, true><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else if (h.interp && h.has_neg && h.layout == CUBE_PAIRS)
+    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_PAIRS, true><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.interp && h.has_neg)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA, true><<<grid, kThreads, 0, s>>>(h, cp, stats);
-  else if (h.interp && h.compact)
+  else if (h.interp && h.layout == CUBE_COMPACT)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else if (h.interp && h.layout == CUBE_PAIRS)
+    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_PAIRS><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, cp, stats);
-  else if (h.compact) render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
+  else if (h.layout != CUBE_RECORDS)
+    render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA><<<grid, kThreads, 0, s>>>(h, cp, stats);
   return cudaGetLastError();
 }
@@ -1805,6 +1867,8 @@ int persistent_grid(int cls) {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI>, kThreads, 0);
   else if (cls == BATCH_CUBE_TRI_COMPACT)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI_COMPACT>, kThreads, 0);
+  else if (cls == BATCH_CUBE_TRI_PAIRS)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CUBE_TRI_PAIRS>, kThreads, 0);
   else if (cls == BATCH_CMEM)
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, render_batch_kernel<BATCH_CMEM>, kThreads, 0);
   else if (cls == BATCH_CUBE_NEAREST)
@@ -1822,6 +1886,7 @@ cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int
   if (model) cp = *model;
   if (cls == BATCH_CUBE_TRI) render_batch_kernel<BATCH_CUBE_TRI><<<grid, kThreads, 0, s>>>(b, cp);
   else if (cls == BATCH_CUBE_TRI_COMPACT) render_batch_kernel<BATCH_CUBE_TRI_COMPACT><<<grid, kThreads, 0, s>>>(b, cp);
+  else if (cls == BATCH_CUBE_TRI_PAIRS) render_batch_kernel<BATCH_CUBE_TRI_PAIRS><<<grid, kThreads, 0, s>>>(b, cp);
   else if (cls == BATCH_CMEM) render_batch_kernel<BATCH_CMEM><<<grid, kThreads, 0, s>>>(b, cp);
   else if (cls == BATCH_CUBE_NEAREST) render_batch_kernel<BATCH_CUBE_NEAREST><<<grid, kThreads, 0, s>>>(b, cp);
   else if (cls == BATCH_CUBE_SIGNED) render_batch_kernel<BATCH_CUBE_SIGNED><<<grid, kThreads, 0, s>>>(b, cp);
@@ -1832,6 +1897,7 @@ cudaError_t launch_render_batch(const BatchDev& b, int grid, cudaStream_t s, int
 const void* render_batch_function(int cls) {
   if (cls == BATCH_CUBE_TRI) return (const void*)render_batch_kernel<BATCH_CUBE_TRI>;
   if (cls == BATCH_CUBE_TRI_COMPACT) return (const void*)render_batch_kernel<BATCH_CUBE_TRI_COMPACT>;
+  if (cls == BATCH_CUBE_TRI_PAIRS) return (const void*)render_batch_kernel<BATCH_CUBE_TRI_PAIRS>;
   if (cls == BATCH_CMEM) return (const void*)render_batch_kernel<BATCH_CMEM>;
   if (cls == BATCH_CUBE_NEAREST) return (const void*)render_batch_kernel<BATCH_CUBE_NEAREST>;
   if (cls == BATCH_CUBE_SIGNED) return (const void*)render_batch_kernel<BATCH_CUBE_SIGNED>;
@@ -1882,6 +1948,14 @@ cudaError_t launch_cube_records(const float* padded, int nx, int ny, int nz, con
   const long long n = (long long)(nx + 1) * (ny + 1) * (nz + 1);
   int blocks = (int)std::min<long long>((n + 255) / 256, 8192);
   cube_records_kernel<<<blocks, 256, 0, s>>>(padded, nx, ny, nz, cx64, cy64, cz64, rec);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cube_pairs(const float* padded, int nx, int ny, int nz, const double* cz64, float2* pairs,
+                              cudaStream_t s) {
+  const long long n = (long long)(nx + 2) * (ny + 2) * (nz + 2);
+  int blocks = (int)std::min<long long>((n + 255) / 256, 8192);
+  cube_pairs_kernel<<<blocks, 256, 0, s>>>(padded, nx, ny, nz, cz64, pairs);
   return cudaGetLastError();
 }
 

@@ -9,8 +9,8 @@
 // from the pinned host copy on that uploader's own stream, with
 // stream-ordered pool allocations so neither upload nor eviction
 // synchronises the device) — the other requests keep being batched
-// meanwhile. With a records share, an idle uploader rebuilds the most
-// requested compact cube in the records layout. Batches on different slots
+// meanwhile. With a promotion share, an idle uploader rebuilds the most
+// requested cube in the faster promoted layout. Batches on different slots
 // overlap on the GPU. One completion thread per slot waits for its batch,
 // copies each image to the caller's buffer unless the kernels wrote it there,
 // and completes the tickets.
@@ -50,8 +50,8 @@ struct Source {
   birp_status upload_err = BIRP_OK;  // the last upload's failure, reported once
   birp_cmem* cmem = nullptr;
   int64_t requests = 0;       // requests submitted for it (the promotion's ranking)
-  int64_t bytes_records = 0;  // device bytes in the records layout
-  bool promoting = false;     // its records copy is being built
+  int64_t bytes_promoted = 0;  // device bytes in the promoted layout
+  bool promoting = false;      // its promoted copy is being built
 };
 
 struct Req {
@@ -92,9 +92,9 @@ struct birp_server {
   int64_t next_ticket = 1;
   uint64_t tick = 0;
   int64_t resident_bytes = 0;
-  int64_t records_bytes = 0;  // resident cubes promoted to the records layout
-  // compact copies replaced by their records copy while batches in flight
-  // still read them: freed when the last of those batches completes
+  int64_t promoted_bytes = 0;  // resident cubes in the promoted layout
+  // copies replaced by their promoted copy while batches in flight still
+  // read them: freed when the last of those batches completes
   std::vector<std::pair<birp_cube*, int>> retired;
   std::vector<cudaStream_t> upload_streams;
   birp_server_stats st{};
@@ -128,7 +128,7 @@ birp_status make_room_bytes(birp_server* s, int64_t need, int keep) {
     birp_cube* c = v.resident;
     v.resident = nullptr;
     s->resident_bytes -= (int64_t)c->device_bytes;
-    if (c->layout == BIRP_CUBE_RECORDS && s->cfg.records_budget_bytes > 0) s->records_bytes -= (int64_t)c->device_bytes;
+    if (c->layout != s->cfg.cube_layout) s->promoted_bytes -= (int64_t)c->device_bytes;
     s->st.cube_evictions++;
     destroy_cube_device(*c);  // stream-ordered release on the upload stream
     delete c;
@@ -153,34 +153,34 @@ void retire_cube(birp_server* s, birp_cube* c) {
   }
 }
 
-// Promotion (records_budget_bytes > 0; uploader thread, lock held on entry
-// and exit): the most-requested resident compact cube whose records copy
-// fits the records share is rebuilt in the records layout from its host
-// copy, with the lock released meanwhile, and takes the compact copy's
-// place. Returns whether it did one.
+// Promotion (promoted_budget_bytes > 0; uploader thread, lock held on entry
+// and exit): the most-requested resident cube of the server's layout whose
+// promoted copy fits the promotion share is rebuilt in the promoted layout
+// from its host copy, with the lock released meanwhile, and takes the other
+// copy's place. Returns whether it did one.
 bool try_promote(birp_server* s, std::unique_lock<std::mutex>& lk, cudaStream_t stream) {
-  if (s->cfg.records_budget_bytes <= 0 || s->cfg.cube_layout != BIRP_CUBE_COMPACT) return false;
+  if (s->cfg.promoted_budget_bytes <= 0) return false;
   int best = -1;
   for (int i = 0; i < (int)s->sources.size(); ++i) {
     const Source& o = s->sources[i];
-    if (o.kind != 0 || !o.resident || o.resident->layout != BIRP_CUBE_COMPACT || o.uploading || o.promoting ||
-        o.requests < 16 || s->records_bytes + o.bytes_records > s->cfg.records_budget_bytes)
+    if (o.kind != 0 || !o.resident || o.resident->layout != s->cfg.cube_layout || o.uploading || o.promoting ||
+        o.requests < 16 || s->promoted_bytes + o.bytes_promoted > s->cfg.promoted_budget_bytes)
       continue;
     if (best < 0 || o.requests > s->sources[best].requests) best = i;
   }
   if (best < 0) return false;
-  // room for the records copy beside the compact one until the swap
-  if (make_room_bytes(s, s->sources[best].bytes_records, best) != BIRP_OK) return false;
+  // room for the promoted copy beside the other one until the swap
+  if (make_room_bytes(s, s->sources[best].bytes_promoted, best) != BIRP_OK) return false;
   Source& src = s->sources[best];
   src.promoting = true;
-  const int64_t reserved = src.bytes_records;
+  const int64_t reserved = src.bytes_promoted;
   s->resident_bytes += reserved;
   const float* vals = src.h_vals;
   const int has_neg = src.has_neg;
   std::vector<double> ax[3] = {src.ax[0], src.ax[1], src.ax[2]};
   lk.unlock();
   birp_cube* c = new birp_cube();
-  c->layout = BIRP_CUBE_RECORDS;
+  c->layout = s->cfg.promoted_layout;
   c->has_neg = has_neg;
   birp_status rc = BIRP_OK;
   for (int k = 0; k < 3 && rc == BIRP_OK; ++k) rc = analyze_axis(ax[k].data(), (int)ax[k].size(), "xyz"[k], *c, k);
@@ -195,10 +195,10 @@ bool try_promote(birp_server* s, std::unique_lock<std::mutex>& lk, cudaStream_t 
     return false;
   }
   s->resident_bytes += (int64_t)c->device_bytes;
-  s->records_bytes += (int64_t)c->device_bytes;
-  done.bytes_records = (int64_t)c->device_bytes;
+  s->promoted_bytes += (int64_t)c->device_bytes;
+  done.bytes_promoted = (int64_t)c->device_bytes;
   birp_cube* old = done.resident;
-  done.resident = c;  // batches formed from now on read the records copy
+  done.resident = c;  // batches formed from now on read the promoted copy
   done.bytes = (int64_t)c->device_bytes;
   retire_cube(s, old);
   s->st.cube_promotions++;
@@ -215,10 +215,10 @@ void uploader_loop(birp_server* s, int idx) {
   std::unique_lock<std::mutex> lk(s->mu);
   while (!s->stop) {
     if (s->upload_q.empty()) {
-      // idle: promote a popular compact cube, else wait for work (and look
-      // again for a promotion now and then)
+      // idle: promote a popular cube, else wait for work (and look again for
+      // a promotion now and then)
       if (try_promote(s, lk, stream)) continue;
-      if (s->cfg.records_budget_bytes > 0) s->cv_upload.wait_for(lk, std::chrono::milliseconds(20));
+      if (s->cfg.promoted_budget_bytes > 0) s->cv_upload.wait_for(lk, std::chrono::milliseconds(20));
       else s->cv_upload.wait(lk);
       continue;
     }
@@ -434,7 +434,8 @@ void birp_server_default_config(birp_server_config* c) {
   c->max_queue = 1 << 16;
   c->max_wait_ms = 1.0;
   c->cube_layout = BIRP_CUBE_RECORDS;
-  c->records_budget_bytes = 0;
+  c->promoted_layout = BIRP_CUBE_RECORDS;
+  c->promoted_budget_bytes = 0;
   c->uploaders = 1;
 }
 
@@ -447,8 +448,13 @@ birp_status birp_server_create(const birp_server_config* cfg, birp_server** out)
   if (cfg) c = *cfg;
   if (c.slots < 1 || c.slots > 16 || c.max_batch_requests < 1 || c.max_batch_pixels < 1 || c.max_queue < 1 ||
       c.cube_budget_bytes < 0 || !(c.max_wait_ms >= 0) ||
-      (c.cube_layout != BIRP_CUBE_RECORDS && c.cube_layout != BIRP_CUBE_COMPACT) || c.records_budget_bytes < 0 ||
-      c.records_budget_bytes > c.cube_budget_bytes || c.uploaders < 1 || c.uploaders > 8)
+      (c.cube_layout != BIRP_CUBE_RECORDS && c.cube_layout != BIRP_CUBE_COMPACT && c.cube_layout != BIRP_CUBE_PAIRS) ||
+      c.promoted_budget_bytes < 0 || c.promoted_budget_bytes > c.cube_budget_bytes || c.uploaders < 1 ||
+      c.uploaders > 8 ||
+      (c.promoted_budget_bytes > 0 &&
+       !(c.promoted_layout == BIRP_CUBE_RECORDS ? c.cube_layout != BIRP_CUBE_RECORDS
+         : c.promoted_layout == BIRP_CUBE_PAIRS  ? c.cube_layout == BIRP_CUBE_COMPACT
+                                                 : false)))
     return fail(BIRP_ERR_INVALID, "bad server configuration");
   birp_server* s = new birp_server();
   s->cfg = c;
@@ -553,9 +559,9 @@ birp_status birp_server_add_cube(birp_server* s, const double* xs, int nx, const
   std::memcpy(src.h_vals, values, count * sizeof(float));
   src.has_neg = probe.has_neg = any_negative(src.h_vals, count) ? 1 : 0;
   src.bytes = (int64_t)cube_device_bytes(probe);
-  birp_cube probe_records = probe;
-  probe_records.layout = BIRP_CUBE_RECORDS;
-  src.bytes_records = (int64_t)cube_device_bytes(probe_records);
+  birp_cube probe_promoted = probe;
+  probe_promoted.layout = s->cfg.promoted_layout;
+  src.bytes_promoted = (int64_t)cube_device_bytes(probe_promoted);
   std::lock_guard<std::mutex> lk(s->mu);
   s->sources.push_back(std::move(src));
   *cube_id = (int)s->sources.size() - 1;
@@ -628,7 +634,7 @@ birp_status birp_server_get_stats(const birp_server* s, birp_server_stats* out) 
   std::lock_guard<std::mutex> lk(m->mu);
   *out = m->st;
   out->resident_bytes = m->resident_bytes;
-  out->records_bytes = m->records_bytes;
+  out->promoted_bytes = m->promoted_bytes;
   return ok();
 }
 

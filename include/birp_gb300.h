@@ -64,10 +64,14 @@ birp_status birp_cube_create(const double* xs, int nx, const double* ys, int ny,
  * nested std::vectors on the host).
  *   RECORDS: one 32-byte record of trilinear coefficients per cell, about 8x
  *            the FP32 values; the fastest to render (the default).
+ *   PAIRS:   per node its FP32 value and the slope of its z-edge, plus a guard
+ *            layer, about 2x; the kernels form a cell's coefficients from its
+ *            4 z-edges (6 differences, 7 products). About 1.2x the records
+ *            layout's render time at a quarter of its memory.
  *   COMPACT: the FP32 node values plus a guard layer, about 1x; the kernels
  *            form each cell's coefficients from its 8 corners. For holding
- *            many cubes under a memory budget (birp_server_config). */
-enum { BIRP_CUBE_RECORDS = 0, BIRP_CUBE_COMPACT = 1 };
+ *            the most cubes under a memory budget (birp_server_config). */
+enum { BIRP_CUBE_RECORDS = 0, BIRP_CUBE_COMPACT = 1, BIRP_CUBE_PAIRS = 2 };
 /* birp_cube_create with an explicit layout. */
 birp_status birp_cube_create_layout(const double* xs, int nx, const double* ys, int ny, const double* zs, int nz,
                                     const float* values, int layout, birp_cube** out);
@@ -77,7 +81,7 @@ typedef struct {
   int nx, ny, nz;
   int uniform[3];          /* 1 where the axis is uniform (affine index) */
   size_t device_bytes;     /* GPU memory held by the cube */
-  int layout;              /* BIRP_CUBE_RECORDS or BIRP_CUBE_COMPACT */
+  int layout;              /* BIRP_CUBE_RECORDS, BIRP_CUBE_COMPACT or BIRP_CUBE_PAIRS */
 } birp_cube_info;
 birp_status birp_cube_get_info(const birp_cube* cube, birp_cube_info* info);
 
@@ -252,14 +256,16 @@ typedef struct {
   int max_queue;               /* pending requests before submit returns BIRP_ERR_BUSY */
   double max_wait_ms;          /* batching window: launch when this old or the batch is full */
   int cube_layout;             /* device layout of the server's cubes (BIRP_CUBE_*) */
-  /* With cube_layout = BIRP_CUBE_COMPACT: the part of cube_budget_bytes that
-   * cubes promoted to the records layout (about 8x the memory, 1.35x faster
-   * to render) may hold; 0 = no promotion. When no upload is waiting, the
-   * most-requested resident compact cube (at least 16 requests) whose
-   * records copy fits that share is rebuilt in the records layout from its
-   * host copy and takes the compact copy's place; the compact copy is freed
-   * once no batch in flight uses it. No counterpart in the reference. */
-  int64_t records_budget_bytes;
+  /* Promotion of popular cubes to a faster layout: promoted_layout
+   * (BIRP_CUBE_RECORDS or BIRP_CUBE_PAIRS, faster than cube_layout) and the
+   * part of cube_budget_bytes the promoted cubes may hold (0 = none). When
+   * no upload is waiting, the most-requested resident cube (at least 16
+   * requests) whose promoted copy fits that share is rebuilt in
+   * promoted_layout from its host copy and takes the other copy's place;
+   * that copy is freed once no batch in flight uses it. No counterpart in the
+   * reference. */
+  int promoted_layout;
+  int64_t promoted_budget_bytes;
   int uploaders;               /* cube uploads in parallel (1..8; one stream each) */
 } birp_server_config;
 
@@ -275,7 +281,7 @@ typedef struct {
   int64_t cube_uploads, cube_evictions, cube_hits;
   int64_t resident_bytes;
   int64_t cube_promotions;     /* compact cubes rebuilt in the records layout */
-  int64_t records_bytes;       /* GPU bytes the promoted cubes hold now */
+  int64_t promoted_bytes;      /* GPU bytes the promoted cubes hold now */
 } birp_server_stats;
 
 void birp_server_default_config(birp_server_config* c);

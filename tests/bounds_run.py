@@ -1,6 +1,6 @@
 """Run by tests/test_gpu_bounds.py in a child process with BIRP_LIB pointing at
 the bounds-checking library: renders every kernel class and edge case the
-walks have (both layouts, both interpolations, both march modes, rays from
+walks have (the three layouts, both interpolations, both march modes, rays from
 inside, outside and along the faces, negative values, thin cells, a far cube
 that tests every sample, CMEM, one mixed batch, the same mix through the
 no-allocation entry point), checks each image against
@@ -49,7 +49,7 @@ def main():
     poses = [((-2.0, -12.0, 16.0), (10.0, 0, 0)), ((1.0, 2.0, 3.0), (9.0, 0, 0)), ((-30.0, 25.0, -35.0), (4.0, 0, 0)),
              ((0.0, 0.0, 0.0), (9.0, 0, 0))]
     for v in fields:
-        for layout in (B.CUBE_RECORDS, B.CUBE_COMPACT):
+        for layout in (B.CUBE_RECORDS, B.CUBE_COMPACT, B.CUBE_PAIRS):
             g = B.Cube(xs, ys, zs, v, layout=layout)
             for tri in (True, False):
                 oc = O.Cube64(xs, ys, zs, v.astype(np.float64), int(tri))
@@ -80,7 +80,7 @@ def main():
     xf = thin_cell_axis(1000.0, 1010.0, 21, 9, 5e-4)
     yf, zf = np.linspace(-1.0, 1.0, 9), np.linspace(-1.0, 1.0, 7)
     sf = np.where(rng.random((len(zf), len(yf), len(xf))) < 0.1, -1.0, 1.0).astype(np.float32)
-    for layout in (B.CUBE_RECORDS, B.CUBE_COMPACT):
+    for layout in (B.CUBE_RECORDS, B.CUBE_COMPACT, B.CUBE_PAIRS):
         gt = B.Cube(xt, yt, zt, vt, layout=layout)
         gf = B.Cube(xf, yf, zf, sf, layout=layout)
         for tri in (True, False):
@@ -102,10 +102,12 @@ def main():
     # one batch mixing every class
     gr = B.Cube(xs, ys, zs, fields[1])
     gc = B.Cube(xs, ys, zs, fields[1], layout=B.CUBE_COMPACT)
+    gp = B.Cube(xs, ys, zs, fields[1], layout=B.CUBE_PAIRS)
     items = []
     for pos, aim in poses:
         items.append((gr, B.camera(pos, aim, 44.0, 36.0, 31, 23, n_samples=700, ray_length=50.0)))
         items.append((gc, B.camera(pos, aim, 44.0, 36.0, 31, 23, n_samples=700, ray_length=50.0)))
+        items.append((gp, B.camera(pos, aim, 44.0, 36.0, 31, 23, n_samples=700, ray_length=50.0)))
         items.append((gr, B.camera(pos, aim, 44.0, 36.0, 31, 23, n_samples=700, ray_length=50.0, trilinear=False)))
         items.append((cm, B.camera(pos, aim, 44.0, 36.0, 15, 11, n_samples=200)))
     b = B.Batch(len(items), sum(c.nx * c.ny for _, c in items))
@@ -126,7 +128,8 @@ def main():
     B.check(fn(B.Batch._reqs(items), len(items), ptrs, None))
     torch.cuda.synchronize()
     o_space = {id(gr): O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 1),
-               id(gc): O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 1), id(cm): O.Cmem64()}
+               id(gc): O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 1),
+               id(gp): O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 1), id(cm): O.Cmem64()}
     o_nearest = O.Cube64(xs, ys, zs, fields[1].astype(np.float64), 0)
     for (sp, cam), d in zip(items, dev):
         img = d.cpu().numpy().reshape(cam.ny, cam.nx)

@@ -40,11 +40,11 @@ def test_cli_arguments_cpu(tmp_path):
     r = subprocess.run([CLI, "-i", str(tmp_path / "cube")], capture_output=True, text=True)
     assert r.returncode == 3
     r = subprocess.run([CLI, "-c", "-m", "bogus"], capture_output=True, text=True)
-    assert r.returncode == 1 and "records or compact" in r.stderr
+    assert r.returncode == 1 and "records, pairs or compact" in r.stderr
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("layout", ["records", "compact"])
+@pytest.mark.parametrize("layout", ["records", "pairs", "compact"])
 def test_cli_batch_directory_matches_batch_api(tmp_path, birp, layout):
     from birp_cpp_gb300 import synth
     _build()
@@ -65,7 +65,7 @@ def test_cli_batch_directory_matches_batch_api(tmp_path, birp, layout):
     assert r.returncode == 0, r.stdout + r.stderr
     assert "Using batch mode" in r.stdout and r.stdout.count("Exported to") == 5
     # the same renders through the batch API (same batch lanes-per-ray table)
-    lay = birp.CUBE_COMPACT if layout == "compact" else birp.CUBE_RECORDS
+    lay = {"records": birp.CUBE_RECORDS, "pairs": birp.CUBE_PAIRS, "compact": birp.CUBE_COMPACT}[layout]
     gcubes = [birp.Cube(*c, layout=lay) for c in cubes]
     cams = [birp.camera((4.0, -9.0, 6.0), (9.0, 0.0, 0.0), 36.0, 36.0, 72, 72, n_samples=200, trilinear=True)
             for _ in cubes]

@@ -142,23 +142,25 @@ def test_server_same_alone_and_in_mix(birp, spaces):
     srv.close()
 
 
-def test_server_promotes_popular_cube(birp):
-    """A compact-layout server with a records share: the cube that gets most
-    requests is rebuilt in the records layout while requests keep arriving;
-    every image, before, during and after the swap, equals the plain render
-    of the same cube in the layout it was rendered from (records after the
-    swap), and the records copy stays within the records share."""
+@pytest.mark.parametrize("base,promoted", [("compact", "records"), ("compact", "pairs"), ("pairs", "records")])
+def test_server_promotes_popular_cube(birp, base, promoted):
+    """A server with a promotion share: the cube that gets most requests is
+    rebuilt in the promoted layout while requests keep arriving; every image,
+    before, during and after the swap, equals the plain render of the same
+    cube in the layout it was rendered from (the promoted one after the
+    swap), and the promoted copy stays within the share."""
     from birp_cpp_gb300 import synth
+    code = {"records": birp.CUBE_RECORDS, "compact": birp.CUBE_COMPACT, "pairs": birp.CUBE_PAIRS}
     cubes = []
     for s in range(3):
         xs, ys, zs, v = synth.cube_config1(seed=60 + s, n=64)
         cubes.append((xs, ys, zs, v.astype(np.float32)))
-    rec = [birp.Cube(*c) for c in cubes]
-    com = [birp.Cube(*c, layout=birp.CUBE_COMPACT) for c in cubes]
-    share = int(1.5 * rec[0].info().device_bytes)  # room for one promoted cube
+    fast = [birp.Cube(*c, layout=code[promoted]) for c in cubes]
+    slow = [birp.Cube(*c, layout=code[base]) for c in cubes]
+    share = int(1.5 * fast[0].info().device_bytes)  # room for one promoted cube
     srv = birp.Server(birp.server_config(cube_budget_bytes=1 << 32, slots=2, max_batch_requests=8,
-                                         max_batch_pixels=1 << 20, max_wait_ms=0.2, cube_layout=birp.CUBE_COMPACT,
-                                         records_budget_bytes=share))
+                                         max_batch_pixels=1 << 20, max_wait_ms=0.2, cube_layout=code[base],
+                                         promoted_layout=code[promoted], promoted_budget_bytes=share))
     ids = [srv.add_cube(*c) for c in cubes]
     cams = [birp.camera(p, a, 27.0, 16.0, 48, 28, n_samples=440, segments=1)
             for p, a, *_ in synth.config2_requests(8, seed=61)]
@@ -178,18 +180,27 @@ def test_server_promotes_popular_cube(birp):
         work.append((0, cam, o, srv.submit(ids[0], cam, o)))
     for k, cam, o, t in work:
         assert srv.wait(t, 30000).status == 0
-        assert np.array_equal(o, birp.render(rec[k], cam)) or np.array_equal(o, birp.render(com[k], cam)), k
+        assert np.array_equal(o, birp.render(fast[k], cam)) or np.array_equal(o, birp.render(slow[k], cam)), k
     st = srv.stats()
     assert st.cube_promotions == 1, st.cube_promotions
-    assert 0 < st.records_bytes <= share
-    # after the swap, cube 0 renders from its records copy
+    assert 0 < st.promoted_bytes <= share
+    # after the swap, cube 0 renders from its promoted copy
     for cam in cams[:4]:
         o = np.empty((cam.ny, cam.nx), np.float32)
         assert srv.wait(srv.submit(ids[0], cam, o), 30000).status == 0
-        assert np.array_equal(o, birp.render(rec[0], cam))
+        assert np.array_equal(o, birp.render(fast[0], cam))
     srv.close()
-    for c in rec + com:
+    for c in fast + slow:
         c.close()
+
+
+def test_server_rejects_bad_promotion(birp):
+    """A promoted layout must be faster than the server's own: records over
+    compact or pairs, pairs over compact."""
+    for base, promoted in [(birp.CUBE_RECORDS, birp.CUBE_RECORDS), (birp.CUBE_RECORDS, birp.CUBE_PAIRS),
+                           (birp.CUBE_PAIRS, birp.CUBE_PAIRS), (birp.CUBE_COMPACT, birp.CUBE_COMPACT)]:
+        with pytest.raises(birp.BirpError):
+            birp.Server(birp.server_config(cube_layout=base, promoted_layout=promoted, promoted_budget_bytes=1 << 30))
 
 
 def test_server_lru_eviction_and_errors(birp, spaces):

@@ -1,7 +1,7 @@
 """Seeded random parity sweep against the FP64 oracle: random nonuniform cubes
 (2 to 24 nodes per axis), random poses inside and outside the box, random
 fields of view, image sizes, sample counts and ray lengths, both march modes,
-both interpolations, both layouts, plain renders and one mixed batch.
+both interpolations, the three layouts, plain renders and one mixed batch.
 Non-negative fields: max relative error <= 1e-5 on pixels above 1e-3 of the
 image maximum and the same dark pixels. Sign-only fields in nearest mode
 (every run cut at its first negative node): bit for bit."""
@@ -52,7 +52,7 @@ def test_random_views_nonnegative(birp, oracle):
     for case in range(48):
         xs, ys, zs, cam = random_case(birp, rng)
         v = rng.uniform(0.0, 5.0, (len(zs), len(ys), len(xs))).astype(np.float32)
-        layout = int(rng.integers(0, 2))
+        layout = int(rng.integers(0, 3))
         g = birp.Cube(xs, ys, zs, v, layout=layout)
         oc = oracle.Cube64(xs, ys, zs, v.astype(np.float64), int(cam.trilinear))
         ref = oracle.render64(oc, o_cam(oracle, cam), threads=THREADS)
@@ -78,7 +78,7 @@ def test_random_sign_fields_nearest_bitwise(birp, oracle):
         xs, ys, zs, cam = random_case(birp, rng)
         cam.trilinear = 0
         s = np.where(rng.random((len(zs), len(ys), len(xs))) < 0.15, -1.0, 1.0).astype(np.float32)
-        layout = int(rng.integers(0, 2))
+        layout = int(rng.integers(0, 3))
         g = birp.Cube(xs, ys, zs, s, layout=layout)
         oc = oracle.Cube64(xs, ys, zs, s.astype(np.float64), 0)
         ref = oracle.render64(oc, o_cam(oracle, cam), threads=THREADS).astype(np.float32)

@@ -72,7 +72,7 @@ def thin_cell_axis(lo, hi, n, thin_at, width):
     return xs
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_thin_cells_signed_field(birp, oracle, layout):
     """A cell 3.2e-5 wide next to cells ~0.13 wide (span / smallest cell just
     under the index-table limit of 65536): nearest-mode crossings of the thin
@@ -101,7 +101,7 @@ def test_thin_cells_signed_field(birp, oracle, layout):
     g.close()
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_far_cube_every_sample_exact(birp, oracle, layout):
     """A cube at x in [1000, 1010] Re with a 5e-4 cell (8 FP32 ulps of 1000):
     the FP32 position of a sample is too coarse to trust its cell within one,
