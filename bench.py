@@ -944,10 +944,10 @@ def main():
             "roofline_per_sample": roofline_per_sample,
             "roofline_hbm": roofline_hbm,
             "cpu_baseline": cpu,
-            # each step replays one graph with five kernels: the CMEM, signed,
-            # nearest and compact-layout ones (no work here) and the
+            # each step replays one graph with six kernels: the CMEM, signed,
+            # nearest, compact- and pairs-layout ones (no work here) and the
             # records-layout trilinear one
-            "gpu_launches": 5 * args.steps, "clocks": clock_summary,
+            "gpu_launches": 6 * args.steps, "clocks": clock_summary,
             "exact_fp64_rays_per_step": ks["exact_range_rays"] / args.steps,
             "samples_per_cell": (ks["samples"] / ks["cells"]) if ks.get("cells") else None,
             "c3": c3, "c4": c4,

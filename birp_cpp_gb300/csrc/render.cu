@@ -751,9 +751,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     if (!certain && valid) {
       int s = 0, e = N;
       bool used64 = false;
-      // the float-float tier pays off in the records trilinear kernel; in the
-      // others its registers cost more than the FP64 searches it saves
-      if constexpr (INTERP == TRILINEAR && AXES == AXES_DDA) {
+      // the float-float tier pays off in the records and pairs trilinear
+      // kernels (pairs: 8.75 -> 8.57 ms on 64 orbit renders); in the others
+      // its registers cost more than the FP64 searches it saves
+      if constexpr (INTERP == TRILINEAR && (AXES == AXES_DDA || AXES == AXES_DDA_PAIRS)) {
         // An axis the FP32 bound leaves undecided is decided in float-float:
         // its interval ends are the first samples past the box's first and
         // last planes, u = P / (d dt) - K as in the nearest walk, with that
@@ -1061,8 +1062,19 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           // pairs of independent FMAs as one packed FP32x2 instruction (the
           // record's float4 halves are the pairs: {c0, c3}, {c1, c5}, {c2,
           // c6}, {c4, c7}); the same roundings as two scalar FMAs
-          const float2 XY = __ffma2_rn(make_float2(u, u), make_float2(st[0], st[1]), make_float2(xb[0], xb[1]));
-          const float X = XY.x, Y = XY.y, Z = fmaf(u, st[2], xb[2]);
+          // (the pairs layout is faster with X and Y as scalar FMAs: 9.13 ->
+          // 8.77 ms on 64 orbit renders; records 7.29 -> 7.80 ms, compact
+          // 10.38 -> 10.79 ms with them)
+          float X, Y;
+          if constexpr (PAIRS) {
+            X = fmaf(u, st[0], xb[0]);
+            Y = fmaf(u, st[1], xb[1]);
+          } else {
+            const float2 XY = __ffma2_rn(make_float2(u, u), make_float2(st[0], st[1]), make_float2(xb[0], xb[1]));
+            X = XY.x;
+            Y = XY.y;
+          }
+          const float Z = fmaf(u, st[2], xb[2]);
           // value, gradient and mixed second derivatives at the first sample:
           // (c0 + c1 X, c3 + c5 X), (c2 + c4 X, c6 + c7 X), then
           // (c0 + c1 X + (c2 + c4 X) Y, c3 + c5 X + (c6 + c7 X) Y) = (f at z = 0, f_z)
@@ -1074,8 +1086,24 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           const float gy = fmaf(a1, Z, a0);
           const float hxy = fmaf(hi.w, Z, hi.z), hxz = fmaf(hi.w, Y, lo.w);  // c4 + c7 Z, c5 + c7 Y
           const float gx = fmaf(hxz, Z, fmaf(hi.z, Y, lo.z));  // c1 + c4 Y + c5 Z + c7 Y Z
-          const float p1 = fmaf(gx, st[0], fmaf(gy, st[1], gz * st[2]));
-          const float p2 = fmaf(hxy, DxDy, fmaf(hxz, DxDz, a1 * DyDz));
+          // the first and second directional derivatives along the ray:
+          // p1 = gx Dx + gy Dy + gz Dz, p2 = hxy DxDy + hxz DxDz + a1 DyDz,
+          // both as packed pairs in the records layout (7.51 -> 7.28 ms on 64
+          // orbit renders of the 256^3 cube); the node-value layouts, whose
+          // coefficient formation also keeps the FMA pipes busy, are faster
+          // with the scalar form (pairs 9.12 / 9.28 ms, compact 10.37 /
+          // 10.68 ms). Same roundings either way.
+          float p1, p2;
+          if constexpr (NODES) {
+            p1 = fmaf(gx, st[0], fmaf(gy, st[1], gz * st[2]));
+            p2 = fmaf(hxy, DxDy, fmaf(hxz, DxDz, a1 * DyDz));
+          } else {
+            float2 P12 = __fmul2_rn(make_float2(gz, a1), make_float2(st[2], DyDz));
+            P12 = __ffma2_rn(make_float2(gy, hxz), make_float2(st[1], DxDz), P12);
+            P12 = __ffma2_rn(make_float2(gx, hxy), make_float2(st[0], DxDy), P12);
+            p1 = P12.x;
+            p2 = P12.y;
+          }
           const float p3 = hi.w * DxDyDz;
           const float s1 = 0.5f * fmaf(m, m, -m);  // m (m - 1) / 2, exact
           const float s2 = s1 * fmaf(m, 2.f / 3.f, -1.f / 3.f);
