@@ -207,6 +207,10 @@ birp_status upload_cube(birp_cube& c, const float* values, cudaStream_t st, bool
   } else {
     CKU(dev_alloc(&c.d_cells, walk2.size() * sizeof(float2), c.alloc_stream));
     CKU(dev_alloc(&c.d_vals, records * 2 * sizeof(float4), c.alloc_stream));
+    // the walk reads a record with one 32-byte load, which needs 32-byte
+    // alignment (device allocations are 256-byte aligned)
+    if (reinterpret_cast<uintptr_t>(c.d_vals) % 32 != 0)
+      return fail(BIRP_ERR_CUDA, "cell records not 32-byte aligned");
   }
   CKU(dev_alloc(&c.d_c64, coords * sizeof(double), c.alloc_stream));
   CKU(dev_alloc(&c.d_nodes_ff, (coords + 6) * sizeof(float2), c.alloc_stream));

@@ -1023,8 +1023,12 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
 #ifdef BIRP_DEBUG_BOUNDS
           if (!bound_ok(q - C.rec, C.rec_f4 - 1, 6)) q = C.rec;
 #endif
-          lo = __ldg(q);
-          hi = __ldg(q + 1);
+          // the 32-byte record in one 256-bit load (records are 32-byte
+          // aligned: the allocation is, and a record is 32 bytes): 7.28 ->
+          // 7.14 ms on 64 orbit renders against two 16-byte loads
+          asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+              : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z), "=f"(hi.w)
+              : "l"(q));
         }
         const float nxt = fminf(ceilf(fminf(fminf(ex[0], ex[1]), ex[2])), ub);
         // a cube holding negative values: a cell next to a negative node
@@ -1106,8 +1110,15 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
           }
           const float p3 = hi.w * DxDyDz;
           const float s1 = 0.5f * fmaf(m, m, -m);  // m (m - 1) / 2, exact
-          const float s2 = s1 * fmaf(m, 2.f / 3.f, -1.f / 3.f);
-          const float s3 = s1 * s1;
+          float s2, s3;
+          if constexpr (COMPACT) {
+            s2 = s1 * fmaf(m, 2.f / 3.f, -1.f / 3.f);
+            s3 = s1 * s1;
+          } else {  // one packed product (records 1 %, pairs 0.4 % faster; compact 3 % slower)
+            const float2 S23 = __fmul2_rn(make_float2(s1, s1), make_float2(fmaf(m, 2.f / 3.f, -1.f / 3.f), s1));
+            s2 = S23.x;
+            s3 = S23.y;
+          }
           acc.add(fmaf(p3, s3, fmaf(p2, s2, fmaf(p1, s1, f0v * m))));
           u = nxt;
           ++ncell;
