@@ -353,11 +353,16 @@ __device__ __forceinline__ float pow_pos(float a, float b) { return ex2_fast(b *
 
 constexpr float kLog2e = 1.4426950408889634f;
 
-// r_mp and r_bs in FP32; mp_terms = |p0 r0 f| + |q|, the size of the two
-// terms whose sum is r_mp (near the cusps q cancels most of the first, and
-// r_mp's absolute FP32 error follows mp_terms, not r_mp).
-__device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d, float& r_mp, float& r_bs,
-                                             float& mp_terms) {
+// The magnetopause radius is r_mp = p0 r0 f + q: the first term without the
+// cusps (cmem_mp_base), q the two cusp indentations (cmem_cusps). The bow
+// shock radius r_bs (cmem_bow_shock). FP32.
+__device__ __forceinline__ float cmem_mp_base(const CmemDev& m, const CmemDir& d) {
+  const float ch = rsqrt_fast(d.b2);  // cos(theta / 2); b2 >= 1
+  float base = ch + m.a5 * (2.f * d.st * d.ct) * (1.f - ex2_fast(-kLog2e * d.theta));
+  float f = pow_pos(base, m.p1 * (m.bc0 + m.bc1 * d.cp + m.bc3 * (d.sp * d.sp)));
+  return m.p0r0 * f;
+}
+__device__ __forceinline__ float cmem_cusps(const CmemDev& m, const CmemDir& d) {
   // angle to the northern / southern cusp axes
   const float ux = d.ct, uy = d.st * d.cp, uz = d.st * d.sp;
   float dn = ux * m.cos_tn + uz * m.sin_tn;
@@ -366,37 +371,71 @@ __device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d,
   float ds = ux * m.cos_ts - uz * m.sin_ts;
   float csx = -uy * m.sin_ts, csy = uz * m.cos_ts + ux * m.sin_ts, csz = -uy * m.cos_ts;
   float phi_s = atan2_pos(sqrt_fast(csx * csx + csy * csy + csz * csz), ds);
-  const float ch = rsqrt_fast(d.b2);  // cos(theta / 2); b2 >= 1
-  float base = ch + m.a5 * (2.f * d.st * d.ct) * (1.f - ex2_fast(-kLog2e * d.theta));
-  float f = pow_pos(base, m.p1 * (m.bc0 + m.bc1 * d.cp + m.bc3 * (d.sp * d.sp)));
-  float q = m.p2c * ex2_fast(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
-            m.p2c * ex2_fast(kLog2e * m.p3ds * pow_pos(phi_s, m.a21));
-  r_mp = m.p0r0 * f + q;
-  mp_terms = fabsf(m.p0r0 * f) + fabsf(q);
+  return m.p2c * ex2_fast(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
+         m.p2c * ex2_fast(kLog2e * m.p3ds * pow_pos(phi_s, m.a21));
+}
+__device__ __forceinline__ float cmem_bow_shock(const CmemDev& m, const CmemDir& d) {
   const float lb = __log2f(d.b2);
   float ry = m.bs * ex2_fast(m.ay * lb);
   float rz = m.bs * ex2_fast(m.az * lb);
   float a1 = rz * d.cp, a2 = ry * d.sp;
-  r_bs = (ry * rz) * rsqrt_fast(a1 * a1 + a2 * a2);  // cp^2 + sp^2 = 1: the sum is > 0
+  return (ry * rz) * rsqrt_fast(a1 * a1 + a2 * a2);  // cp^2 + sp^2 = 1: the sum is > 0
+}
+
+// r_mp and r_bs in FP32; mp_terms = |p0 r0 f| + |q|, the size of the two
+// terms whose sum is r_mp (near the cusps q cancels most of the first, and
+// r_mp's absolute FP32 error follows mp_terms, not r_mp).
+__device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d, float& r_mp, float& r_bs,
+                                             float& mp_terms) {
+  const float base = cmem_mp_base(m, d);
+  const float q = cmem_cusps(m, d);
+  r_mp = base + q;
+  mp_terms = fabsf(base) + fabsf(q);
+  r_bs = cmem_bow_shock(m, d);
 }
 
 __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
   const CmemDir d = cmem_dir32(x, y, z);
-  float r_mp, r_bs, mp_terms;
-  cmem_radii32(m, d, r_mp, r_bs, mp_terms);
   const float r = d.r;
   const float half = 0.025f;
   CmemEval out;
   float tol = fmaf(m.eps_rel, r + 5.f, perr);
-  out.unsure = !(fabsf(r - (r_mp + half)) > tol) || !(fabsf(r - (r_bs + half)) > tol);
-  // the shell the sample is in, by the reference's branch chain (NaN radii
-  // fall through it as there); the sheath and outer emissivities are
-  // computed only where the shell uses them
-  const int shell = (r < r_mp - half)                        ? 0
-                    : (r >= r_mp - half && r <= r_mp + half) ? 1
-                    : (r > r_mp + half && r < r_bs - half)   ? 2
-                    : (r >= r_bs - half && r <= r_bs + half) ? 3
-                                                             : 4;
+  // Radii only as far as the shell needs them, with the decisions of the
+  // full computation: with p2c <= 0 every cusp term is <= 0 in FP32 too, so
+  // r_mp <= p0 r0 f, and a sample more than half + tol beyond p0 r0 f is
+  // past the magnetopause's upper edge whatever q is (shell 2, 3 or 4, the
+  // r_mp test of `unsure` false): q is not needed. A sample more than
+  // half + tol inside r_mp is in shell 0, away from every discontinuity the
+  // value has there (a bow shock inside it would flag it for the FP64 path,
+  // which returns 0 there too): r_bs is not needed.
+  const float mp_base = cmem_mp_base(m, d);
+  float r_mp = mp_base, r_bs = 0.f, mp_terms = 0.f;
+  int shell;
+  if (m.p2c <= 0.f && r - (half + tol) > mp_base) {
+    r_bs = cmem_bow_shock(m, d);
+    out.unsure = !(fabsf(r - (r_bs + half)) > tol);
+    shell = (r < r_bs - half) ? 2 : (r >= r_bs - half && r <= r_bs + half) ? 3 : 4;
+  } else {
+    const float q = cmem_cusps(m, d);
+    r_mp = mp_base + q;
+    mp_terms = fabsf(mp_base) + fabsf(q);
+    if (r < r_mp - (half + tol)) {
+      out.unsure = false;
+      shell = 0;
+    } else {
+      r_bs = cmem_bow_shock(m, d);
+      out.unsure = !(fabsf(r - (r_mp + half)) > tol) || !(fabsf(r - (r_bs + half)) > tol);
+      // the shell the sample is in, by the reference's branch chain (NaN
+      // radii fall through it as there)
+      shell = (r < r_mp - half)                        ? 0
+              : (r >= r_mp - half && r <= r_mp + half) ? 1
+              : (r > r_mp + half && r < r_bs - half)   ? 2
+              : (r >= r_bs - half && r <= r_bs + half) ? 3
+                                                       : 4;
+    }
+  }
+  // the sheath and outer emissivities are computed only where the shell uses
+  // them
   float sheath = 0.f, outer = 0.f;
   if (shell >= 1 && shell <= 3) {
     const float h = 0.5f * d.theta;
