@@ -87,7 +87,7 @@ def main():
             for march in (B.PREFIX, B.CLIP):
                 check(O.Cube64(xt, yt, zt, vt.astype(np.float64), int(tri)), gt,
                       B.camera((0.05, 0.02, 0.01), (1.9, 0, 0), 40.0, 40.0, 29, 23, n_samples=3000, ray_length=4.0,
-                               trilinear=tri, march=march), 5e-5)
+                               trilinear=tri, march=march), 1e-5)
                 n_img += 1
             check(O.Cube64(xf, yf, zf, sf.astype(np.float64), 0), gf,
                   B.camera((1000.2, 0.1, 0.05), (1009.0, 0, 0), 20.0, 20.0, 21, 17, n_samples=4000, ray_length=10.0,

@@ -97,7 +97,7 @@ def test_thin_cells_signed_field(birp, oracle, layout):
                 img = birp.render(g, cam)
                 ref = oracle.render64(oc, o_cam(oracle, cam), threads=THREADS)
                 mx, rms, n = rel_err(img, ref)
-                assert mx <= 5e-5 and np.array_equal(img == 0, ref == 0), (tri, march, pos, mx, n)
+                assert mx <= 1e-5 and np.array_equal(img == 0, ref == 0), (tri, march, pos, mx, n)
     g.close()
 
 
