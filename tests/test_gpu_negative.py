@@ -2,8 +2,8 @@
 first sample < 0 (src/Camera.cpp:205-209): the -1 it returns outside the box
 and a negative field value alike. The GPU path must cut every run at the
 same sample as the FP64 oracle (PREFIX: the first negative sample; CLIP:
-skip negative samples to the first good one, stop at the next), in both
-layouts, both interpolations, plain and batched.
+skip negative samples to the first good one, stop at the next), in every
+layout, both interpolations, plain and batched.
 
 Stop decisions are exact: a sign-only field in nearest mode makes every
 pixel (run length) * K, bit for bit. Sums: a run now ends at a zero crossing,
@@ -65,7 +65,7 @@ def sc():
     return signed_cube()
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_ill_conditioned_signed_field(birp, oracle, layout):
     """Full-amplitude mixed-sign noise: the stop decisions stay exact (same
     dark pixels), the sums within the signed-field bound."""
@@ -84,7 +84,7 @@ def test_ill_conditioned_signed_field(birp, oracle, layout):
     g.close()
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 @pytest.mark.parametrize("tri", [True, False])
 def test_signed_cube_plain(birp, oracle, sc, layout, tri):
     xs, ys, zs, v = sc
@@ -106,7 +106,7 @@ def test_signed_cube_plain(birp, oracle, sc, layout, tri):
     g.close()
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_signed_cube_batched_and_segments(birp, oracle, sc, layout):
     """One batch mixing the signed cube (every lanes-per-ray split) with a
     non-negative cube; each image against the oracle."""
@@ -143,7 +143,7 @@ def test_signed_cube_batched_and_segments(birp, oracle, sc, layout):
     gp.close()
 
 
-@pytest.mark.parametrize("layout", [0, 1])
+@pytest.mark.parametrize("layout", [0, 1, 2])
 def test_nearest_sign_decisions_bitwise(birp, oracle, sc, layout):
     """Nearest mode over the signs of the signed cube (+1, -1): a pixel is
     (length of its run) * K, so bitwise equality with the FP64 oracle proves
