@@ -272,6 +272,7 @@ struct CmemEval {
 // birp_cmem_margin_check.
 struct CmemDir {
   float r, theta, ct, st, cp, sp, b2;  // b2 = 2 / (1 + cos theta)
+  float x, ryz;                        // for theta (cmem_theta)
 };
 
 // One-instruction base-2 exponential and reciprocal square root (PTX
@@ -321,31 +322,45 @@ __device__ __forceinline__ float atan2_pos(float y, float x) {
 // exact 0 at 0, where x * rsqrt(x) would be 0 * inf)
 __device__ __forceinline__ float sqrt_fast(float x) { return x > 0.f ? x * rsqrt_fast(x) : 0.f; }
 
-__device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
+// The direction terms of a position without theta (cmem_theta adds it):
+// the reciprocal lengths 1/r and 1/r_yz are the hardware reciprocal square
+// roots that also give r and r_yz.
+__device__ __forceinline__ CmemDir cmem_dir32_partial(float x, float y, float z) {
   CmemDir d;
   const float ryz2 = fmaf(y, y, z * z);
-  const float ryz = sqrt_fast(ryz2);
-  d.r = sqrt_fast(fmaf(x, x, ryz2));
+  const float iyz = rsqrt_fast(ryz2);
+  const float ryz = ryz2 > 0.f ? ryz2 * iyz : 0.f;
+  const float r2 = fmaf(x, x, ryz2);
+  const float ir = rsqrt_fast(r2);
+  d.r = r2 > 0.f ? r2 * ir : 0.f;
+  d.x = x;
+  d.ryz = ryz;
+  d.theta = 0.f;
   if (x != 0.f) {
-    d.theta = atan2_pos(ryz, x);
-    const float ir = __fdividef(1.f, d.r);
     d.ct = x * ir;
     d.st = ryz * ir;
     d.b2 = x >= 0.f ? __fdividef(2.f * d.r, d.r + x) : __fdividef(2.f * d.r * (d.r - x), ryz2);
   } else {
-    d.theta = 0.f;
     d.ct = 1.f;
     d.st = 0.f;
     d.b2 = 1.f;
   }
   if (y != 0.f) {
-    const float iyz = __fdividef(1.f, ryz);
     d.cp = y * iyz;
     d.sp = fabsf(z) * iyz;
   } else {
     d.cp = 1.f;
     d.sp = 0.f;
   }
+  return d;
+}
+
+// theta = acos(x / r) as atan2(r_yz, x); 0 where x == 0 (the reference's quirk)
+__device__ __forceinline__ float cmem_theta(const CmemDir& d) { return d.x != 0.f ? atan2_pos(d.ryz, d.x) : 0.f; }
+
+__device__ __forceinline__ CmemDir cmem_dir32(float x, float y, float z) {
+  CmemDir d = cmem_dir32_partial(x, y, z);
+  d.theta = cmem_theta(d);
   return d;
 }
 
@@ -374,6 +389,19 @@ __device__ __forceinline__ float cmem_cusps(const CmemDev& m, const CmemDir& d) 
   return m.p2c * ex2_fast(kLog2e * m.p3dn * pow_pos(phi_n, m.a21)) +
          m.p2c * ex2_fast(kLog2e * m.p3ds * pow_pos(phi_s, m.a21));
 }
+// An upper bound of p0 r0 f from cos(theta / 2) alone (p0 r0 > 0): f =
+// base^e with base = cos(theta / 2) + a5 sin 2theta (1 - exp(-theta)) within
+// |a5| of cos(theta / 2) and e the same exponent, so base^e is at most that
+// power of cos(theta / 2) -/+ 1.001 |a5| (as e < 0 or not); the 1e-5 factor
+// covers the approximate logarithm and exponential. Infinite where that base
+// is not positive (towards the tail, where f grows without bound).
+__device__ __forceinline__ float cmem_mp_base_upper(const CmemDev& m, const CmemDir& d) {
+  const float ch = rsqrt_fast(d.b2);
+  const float e = m.p1 * (m.bc0 + m.bc1 * d.cp + m.bc3 * (d.sp * d.sp));
+  const float b = e < 0.f ? ch - 1.001f * fabsf(m.a5) : ch + 1.001f * fabsf(m.a5);
+  return b > 0.f ? 1.00001f * (m.p0r0 * pow_pos(b, e)) : INFINITY;
+}
+
 __device__ __forceinline__ float cmem_bow_shock(const CmemDev& m, const CmemDir& d) {
   const float lb = __log2f(d.b2);
   float ry = m.bs * ex2_fast(m.ay * lb);
@@ -395,11 +423,30 @@ __device__ __forceinline__ void cmem_radii32(const CmemDev& m, const CmemDir& d,
 }
 
 __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, float y, float z, float perr) {
-  const CmemDir d = cmem_dir32(x, y, z);
+  CmemDir d = cmem_dir32_partial(x, y, z);
   const float r = d.r;
   const float half = 0.025f;
   CmemEval out;
   float tol = fmaf(m.eps_rel, r + 5.f, perr);
+  // Far outside (p2c <= 0, p0 r0 > 0): a sample more than half + tol beyond
+  // the bow shock and beyond an upper bound of p0 r0 f (>= r_mp) is in shell 4
+  // with `unsure` false, as the full computation below decides it (its
+  // "beyond the magnetopause" branch, the same r_bs); theta, the
+  // magnetopause and the sheath are not needed. Only tried past the nose's
+  // bow-shock distance bs, inside which r_bs lies beyond r.
+  float r_bs_pre = 0.f;
+  bool have_bs = false;
+  if (m.p2c <= 0.f && m.p0r0 > 0.f && r - (half + tol) > m.bs) {
+    r_bs_pre = cmem_bow_shock(m, d);
+    have_bs = true;
+    if (r - (half + tol) > r_bs_pre && r - (half + tol) > cmem_mp_base_upper(m, d)) {
+      const float d10 = r * 0.1f;
+      out.unsure = false;
+      out.v = __fdividef(m.A2, d10 * d10 * d10);
+      return out;
+    }
+  }
+  d.theta = cmem_theta(d);
   // Radii only as far as the shell needs them, with the decisions of the
   // full computation: with p2c <= 0 every cusp term is <= 0 in FP32 too, so
   // r_mp <= p0 r0 f, and a sample more than half + tol beyond p0 r0 f is
@@ -412,7 +459,7 @@ __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, floa
   float r_mp = mp_base, r_bs = 0.f, mp_terms = 0.f;
   int shell;
   if (m.p2c <= 0.f && r - (half + tol) > mp_base) {
-    r_bs = cmem_bow_shock(m, d);
+    r_bs = have_bs ? r_bs_pre : cmem_bow_shock(m, d);
     out.unsure = !(fabsf(r - (r_bs + half)) > tol);
     shell = (r < r_bs - half) ? 2 : (r >= r_bs - half && r <= r_bs + half) ? 3 : 4;
   } else {
@@ -423,7 +470,7 @@ __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, floa
       out.unsure = false;
       shell = 0;
     } else {
-      r_bs = cmem_bow_shock(m, d);
+      r_bs = have_bs ? r_bs_pre : cmem_bow_shock(m, d);
       out.unsure = !(fabsf(r - (r_mp + half)) > tol) || !(fabsf(r - (r_bs + half)) > tol);
       // the shell the sample is in, by the reference's branch chain (NaN
       // radii fall through it as there)
@@ -438,9 +485,10 @@ __device__ __forceinline__ CmemEval cmem_value32(const CmemDev& m, float x, floa
   // them
   float sheath = 0.f, outer = 0.f;
   if (shell >= 1 && shell <= 3) {
+    // A1 exp(-B (theta/2)^4) (r/10)^(-alpha - beta sin^2 theta), one exponential
     const float h = 0.5f * d.theta;
     const float h4 = (h * h) * (h * h);
-    sheath = m.A1 * ex2_fast(-kLog2e * m.B * h4) * pow_pos(r * 0.1f, -m.alpha - m.beta * (d.st * d.st));
+    sheath = m.A1 * ex2_fast(fmaf(-kLog2e * m.B, h4, (-m.alpha - m.beta * (d.st * d.st)) * __log2f(r * 0.1f)));
   }
   if (shell >= 3) {
     const float d10 = r * 0.1f;
