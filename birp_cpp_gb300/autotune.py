@@ -187,7 +187,7 @@ CLASSES = {  # class: (macro, candidates of resident CTAs per SM, profile case)
     "compact": ("BIRP_COMPACT_MINB", [5, 6, 7, 8], "compact"),
     "pairs": ("BIRP_PAIRS_MINB", [6, 7, 8], "pairs"),
     "nearest": ("BIRP_NEAREST_MINB", [6, 7, 8], "nearest"),
-    "cmem": ("BIRP_CMEM_MINB", [4, 5, 6, 7], "cmem"),
+    "cmem": ("BIRP_CMEM_MINB", [5, 6, 7, 8, 9, 10, 12], "cmem"),
 }
 
 
