@@ -1577,6 +1577,18 @@ __global__ void __launch_bounds__(kThreads) render_plain_kernel(const __grid_con
                                           KIND == SPACE_CMEM ? &model : nullptr);
 }
 
+// The nearest and compact-layout trilinear marches alone, compiled for the
+// resident CTAs per SM of their batch classes (16 orbit renders, one call
+// each: nearest 4.82 -> 4.58 ms, compact 4.62 -> 4.48 ms; CMEM at its batch
+// class's count was slower with the plain tile shape, 31.1 -> 33.8 ms, and
+// the records and pairs marches no faster).
+template <int INTERP, int AXES, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) render_plain_cube_kernel(const __grid_constant__ RequestDev req,
+                                                                           KernelStats* stats) {
+  __shared__ TileSmem sm;
+  render_tile<SPACE_CUBE, INTERP, AXES>(req, blockIdx.x, blockIdx.y, sm, stats);
+}
+
 // Dispatch over the request's variant.
 __device__ void render_tile_any(const RequestDev& R, int tx, int ty, TileSmem& sm, KernelStats* st) {
   if (R.kind == SPACE_CMEM) {
@@ -1975,13 +1987,13 @@ cudaError_t launch_render_plain(const RequestDev& h, KernelStats* stats, cudaStr
   else if (h.interp && h.has_neg)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA, true><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.interp && h.layout == CUBE_COMPACT)
-    render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
+    render_plain_cube_kernel<TRILINEAR, AXES_DDA_COMPACT, BIRP_COMPACT_MINB><<<grid, kThreads, 0, s>>>(h, stats);
   else if (h.interp && h.layout == CUBE_PAIRS)
     render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA_PAIRS><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.interp) render_plain_kernel<SPACE_CUBE, TRILINEAR, AXES_DDA><<<grid, kThreads, 0, s>>>(h, cp, stats);
   else if (h.layout != CUBE_RECORDS)
-    render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA_COMPACT><<<grid, kThreads, 0, s>>>(h, cp, stats);
-  else render_plain_kernel<SPACE_CUBE, NEAREST, AXES_DDA><<<grid, kThreads, 0, s>>>(h, cp, stats);
+    render_plain_cube_kernel<NEAREST, AXES_DDA_COMPACT, BIRP_NEAREST_MINB><<<grid, kThreads, 0, s>>>(h, stats);
+  else render_plain_cube_kernel<NEAREST, AXES_DDA, BIRP_NEAREST_MINB><<<grid, kThreads, 0, s>>>(h, stats);
   return cudaGetLastError();
 }
 
