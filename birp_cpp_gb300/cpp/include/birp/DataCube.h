@@ -21,6 +21,16 @@ class DataCube : public Space {
   // (values[(k*ny + j)*nx + i] = slices[k][j][i]).
   void Init(const std::vector<double>& xs, const std::vector<double>& ys, const std::vector<double>& zs,
             const std::vector<float>& values);
+  // Builds the cube from another Space sampled at the nodes of the given axes
+  // (src.GetSample at every node, on `threads` host threads, so the Space's
+  // GetSample must then be safe to call concurrently, as the reference's
+  // spaces are): a user-defined Space, which has no GPU representation of
+  // its own, renders on the GPU as this cube, interpolated between the nodes
+  // (a -1 that GetSample returns outside its domain ends a ray there, as the
+  // reference's render does). No counterpart in the reference, whose Camera
+  // calls GetSample per ray sample.
+  void InitFromSpace(Space& src, const std::vector<double>& xs, const std::vector<double>& ys,
+                     const std::vector<double>& zs, int threads = 1);
   // Parses an exported MHD .dat file (src/DataCube.cpp:28-138 format).
   void Load(std::string filename, bool debug);
   float GetSample(float x, float y, float z) override;

@@ -12,7 +12,8 @@ class Space {
   virtual void Init() = 0;
   virtual float GetSample(float x, float y, float z) = 0;
   // GPU representation (exactly one is non-null for the built-in spaces). A
-  // user-defined Space without one cannot be rendered: there is no CPU path.
+  // user-defined Space without one cannot be rendered directly (there is no
+  // CPU path); DataCube::InitFromSpace samples it onto a grid that renders.
   virtual const birp_cube* GpuCube() { return nullptr; }
   virtual const birp_cmem* GpuCmem() { return nullptr; }
   virtual bool Trilinear() const { return false; }

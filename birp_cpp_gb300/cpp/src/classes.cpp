@@ -92,6 +92,28 @@ void DataCube::Init(const std::vector<double>& xs, const std::vector<double>& ys
   }
 }
 
+void DataCube::InitFromSpace(Space& src, const std::vector<double>& xs, const std::vector<double>& ys,
+                             const std::vector<double>& zs, int threads) {
+  if (&src == static_cast<Space*>(this)) throw std::invalid_argument("a cube cannot be sampled from itself");
+  const size_t nx = xs.size(), ny = ys.size(), nz = zs.size();
+  std::vector<float> vals(nx * ny * nz);
+  const int nt = (int)std::max<size_t>(1, std::min<size_t>((size_t)std::max(threads, 1), nz));
+  auto slab = [&](int t) {  // z slabs t, t + nt, ...
+    for (size_t k = (size_t)t; k < nz; k += (size_t)nt)
+      for (size_t j = 0; j < ny; ++j)
+        for (size_t i = 0; i < nx; ++i)
+          vals[(k * ny + j) * nx + i] = src.GetSample((float)xs[i], (float)ys[j], (float)zs[k]);
+  };
+  if (nt == 1) {
+    slab(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(slab, t);
+    for (std::thread& th : pool) th.join();
+  }
+  Init(xs, ys, zs, vals);
+}
+
 namespace {
 
 bool is_space(char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r' || c == '\v' || c == '\f'; }
@@ -406,7 +428,9 @@ namespace {
 void gpu_source(Space* s, const birp_cube*& cube, const birp_cmem*& cmem) {
   cube = s->GpuCube();
   cmem = cube ? nullptr : s->GpuCmem();
-  if (!cube && !cmem) throw std::invalid_argument("this Space has no GPU representation (DataCube or CMEM)");
+  if (!cube && !cmem)
+    throw std::invalid_argument(
+        "this Space has no GPU representation (DataCube or CMEM); DataCube::InitFromSpace samples it onto a grid");
 }
 
 // the reference accumulates into image (src/Camera.cpp:223)

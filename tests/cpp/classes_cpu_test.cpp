@@ -1,5 +1,6 @@
-// The C++ drop-in classes' host-only parts: the .dat loader and the FITS
-// writer (no GPU is touched). argv[1] = output directory.
+// The C++ drop-in classes' host-only parts: the .dat loader, a cube sampled
+// from a user-defined Space, and the FITS writer (no GPU is touched).
+// argv[1] = output directory.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -11,6 +12,15 @@
 #include "birp/Camera.h"
 #include "birp/Cmem.h"
 #include "birp/DataCube.h"
+
+// A user-defined Space, as the reference's tests define one (CubeFake in
+// tests/Camera_test.cpp:25-29 returns 1): here an affine field, -1 outside a
+// slab, as the reference's spaces mark their outside.
+class AffineSpace : public Space {
+ public:
+  void Init() override {}
+  float GetSample(float x, float y, float z) override { return z > 2.5f ? -1.f : 1.f + 0.5f * x - 0.25f * y + z; }
+};
 
 static void write_cube(const std::string& path, const std::string& dims_and_body) {
   std::ofstream f(path);
@@ -105,6 +115,31 @@ int main(int argc, char** argv) {
     threw = true;
   }
   fails += !threw;
+  // a user-defined Space sampled at the nodes (one and several host threads:
+  // the same values), GetSample's -1 kept
+  {
+    AffineSpace src;
+    const std::vector<double> xs = {-2, -1, 0.5, 3}, ys = {-1, 1, 2}, zs = {0, 1, 2, 3, 4};
+    DataCube one, many;
+    one.InitFromSpace(src, xs, ys, zs);
+    many.InitFromSpace(src, xs, ys, zs, 3);
+    fails += !(one.size.x == 4 && one.size.y == 3 && one.size.z == 5);
+    for (size_t k = 0; k < zs.size(); ++k)
+      for (size_t j = 0; j < ys.size(); ++j)
+        for (size_t i = 0; i < xs.size(); ++i) {
+          const float want = src.GetSample((float)xs[i], (float)ys[j], (float)zs[k]);
+          fails += one.slices[k][j][i] != want;
+          fails += many.slices[k][j][i] != want;
+        }
+    fails += one.slices[4][0][0] != -1.f;
+    bool self = false;
+    try {
+      one.InitFromSpace(one, xs, ys, zs);
+    } catch (const std::invalid_argument&) {
+      self = true;
+    }
+    fails += !self;
+  }
   // FITS output of a known image
   CMEM m;  // not initialised: no GPU use
   Camera cam(m, 1.0f, 3.0f, 4.0f);

@@ -224,6 +224,44 @@ static void camera_roll() {
   CHECK(mx > 0);
 }
 
+// The reference's own test space (tests/Camera_test.cpp:25-29: GetSample
+// returns 1), rendered on the GPU through a cube sampled from it that holds
+// every ray: each pixel is 200 samples of 1 times the scale, 2204113.13 in
+// FP64 (the reference's FP32 sum gives 2204118).
+class CubeFake : public Space {
+ public:
+  void Init() override {}
+  float GetSample(float, float, float) override { return 1.f; }
+};
+
+static void user_defined_space() {
+  CubeFake fake;
+  const std::vector<double> ax = {-100.0, 0.0, 100.0};
+  DataCube cube;
+  cube.InitFromSpace(fake, ax, ax, ax, 2);
+  cube.SetTrilinear(true);
+  Camera cam(cube, 0.25f, 36.f, 36.f);
+  float px = 1.f, py = 2.f, pz = 3.f;
+  cam.SetPosition(px, py, pz);
+  cam.SetAim(9.f, 0.f, 0.f);
+  cam.Render();
+  const float first = cam.image[0][0];
+  bool same = true;
+  for (auto& row : cam.image)
+    for (float v : row) same = same && v == first;
+  CHECK(same);
+  CHECK(std::fabs(first - 2204113.13) < 0.5);
+  // a Space with no GPU representation of its own is still refused by Render
+  Camera direct(fake, 0.25f, 36.f, 36.f);
+  bool threw = false;
+  try {
+    direct.Render();
+  } catch (const std::invalid_argument&) {
+    threw = true;
+  }
+  CHECK(threw);
+}
+
 int main(int argc, char** argv) {
   std::string dir = argc > 1 ? argv[1] : ".";
   cmem_basic();
@@ -232,6 +270,7 @@ int main(int argc, char** argv) {
   camera_files_and_accumulation(dir);
   concurrent_cameras();
   camera_roll();
+  user_defined_space();
   std::printf("%d failures\n", failures);
   return failures;
 }
