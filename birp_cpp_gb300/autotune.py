@@ -7,11 +7,13 @@ launch), over
     the arrangement of the CTA's 4 warps over the pixel tile (4x1, 2x2, 1x4),
     tiles up to 32 pixels a side;
       - for a request rendered alone (plain renders of the 256^3 stretched
-        cube from orbit poses), per image-size and sample-count class;
-      - for a request inside a batch (32-request batches of one class), per
-        class, for trilinear and nearest cube requests and for CMEM requests;
+        cube and of the default CMEM model from orbit poses), per
+        image-size and sample-count class, cube and CMEM requests apart;
+      - for a request inside a batch: 32-request batches of one class for
+        trilinear and nearest cube requests, a 16-request batch of mixed
+        sizes for CMEM requests;
   * the resident CTAs per SM each persistent batch kernel class is compiled
-    for (records-layout trilinear, compact-layout trilinear, nearest, CMEM):
+    for (records, pairs and compact-layout trilinear, nearest, CMEM):
     the library is rebuilt with each candidate and the class's batch kernel
     timed on a fixed workload (64 orbit requests; 16 for CMEM) in a child
     process.
@@ -79,11 +81,12 @@ def _timer(B, kind):
     return space, time_plain
 
 
-def tune_plain(n_poses: int = 4, repeats: int = 3):
-    """{(pixels, samples): (best (S, wx, gx), times)} for plain renders."""
+def tune_plain(n_poses: int = 4, repeats: int = 3, kind: str = "cube"):
+    """{(pixels, samples): (best (S, wx, gx), times)} for plain renders of
+    the 256^3 cube (kind "cube") or the default CMEM model ("cmem")."""
     import birp_cpp_gb300 as B
     from birp_cpp_gb300 import synth
-    _space, time_plain = _timer(B, "cube")
+    _space, time_plain = _timer(B, kind)
     poses = [(p, a) for p, a, *_ in synth.config2_requests(n_poses, seed=77)]
     results = {}
     for nx, ny in SIZES:
@@ -100,7 +103,7 @@ def tune_plain(n_poses: int = 4, repeats: int = 3):
             best = min(times, key=times.get)
             results[(nx * ny, n)] = (best, times)
             default = (best[0], 1 << [3, 2, 2, 1][SEGMENTS.index(best[0])], 2)  # the untuned shape of that S
-            print(json.dumps({"context": "plain", "pixels": nx * ny, "n_samples": n, "best": best,
+            print(json.dumps({"context": f"plain {kind}", "pixels": nx * ny, "n_samples": n, "best": best,
                               "ms_best": round(times[best], 4), "ms_default_shape": round(times[default], 4)}),
                   flush=True)
     return results
@@ -143,6 +146,35 @@ def tune_batch(kind: str, batch_size: int = 32, repeats: int = 3, sizes=SIZES, s
     return results
 
 
+def tune_batch_cmem(repeats: int = 3):
+    """{(pixels, samples): (best (S, wx, gx), times)}, one entry standing for
+    every size: 16 orbit requests of mixed sizes on the default CMEM model
+    in one batch, every tile shape of 1, 2, 4 and 8 lanes per ray."""
+    import birp_cpp_gb300 as B
+    from birp_cpp_gb300 import synth
+    space = B.Cmem()
+    reqs = synth.config2_requests(16, seed=2)
+    batch = B.Batch(len(reqs), len(reqs) * 1024 * 600)
+    times = {}
+    for s in SEGMENTS:
+        for wx, gx in shapes(s):
+            items = [(space, B.camera(p, a, synth.FOV_W, synth.FOV_H, nx, ny, n_samples=synth.n_samples(st),
+                                      ray_length=synth.RAY_LENGTH, segments=s, warp_rays_x=wx, tile_warps_x=gx))
+                     for p, a, nx, ny, st in reqs]
+            ms = []
+            for _ in range(repeats + 1):
+                B.flush_l2()
+                batch.submit(items)
+                batch.wait()
+                ms.append(batch.last_ms()[0])
+            times[(s, wx, gx)] = float(np.median(ms[1:]))
+    batch.close()
+    best = min(times, key=times.get)
+    print(json.dumps({"context": "batch cmem (16 orbit requests)", "best": best, "ms_best": round(times[best], 4)}),
+          flush=True)
+    return {(1024 * 600, 880): (best, times)}
+
+
 def _rows(results, kind_code=-1, trilinear=-1, all_sizes=False):
     """Rows ordered by pixels then samples; each row covers pixels up to its
     class (and the geometric midpoint to the next class). all_sizes: one
@@ -164,16 +196,17 @@ def _rows(results, kind_code=-1, trilinear=-1, all_sizes=False):
     return out
 
 
-def write_table(plain, batch_tri, batch_near, batch_cmem, path):
+def write_table(plain, plain_cmem, batch_tri, batch_near, batch_cmem, path):
     lines = ["// Tile-shape tables: the first row whose bounds hold gives the shape.",
              "// Columns: max pixels, max samples, kind (0 cube, 1 CMEM, -1 any), trilinear",
              "// (-1 any), log2(lanes per ray), log2(rays across a warp block), log2(warps",
              "// across a tile) (-1: the default for the lanes per ray). Written by",
              "// birp_cpp_gb300/autotune.py from timings on a GB300 (256^3 stretched cube or",
              "// the default CMEM model, orbit poses, L2 flushed before each launch): plain",
-             "// renders for a request alone, 32-request batches of one class (8 for CMEM)",
-             "// for a request inside a batch.",
-             "static const TuneRow kTuneRowsPlain[] = {"] + _rows(plain) + ["};",
+             "// renders for a request alone (CMEM and cube requests), 32-request batches of",
+             "// one cube class and a 16-request mixed-size CMEM batch for a request inside",
+             "// a batch.",
+             "static const TuneRow kTuneRowsPlain[] = {"] + _rows(plain_cmem, 1, -1) + _rows(plain) + ["};",
              "static const TuneRow kTuneRowsBatch[] = {"] + _rows(batch_cmem, 1, -1, all_sizes=True) + \
             _rows(batch_near, 0, 0) + _rows(batch_tri, -1, -1) + ["};"]
     with open(path, "w") as f:
@@ -284,11 +317,11 @@ def main():
         build.build()
         B.init(0)
         plain = tune_plain(args.poses, args.repeats)
+        plain_cmem = tune_plain(args.poses, args.repeats, kind="cmem")
         tri = tune_batch("tri", repeats=args.repeats)
         near = tune_batch("nearest", repeats=args.repeats)
-        cm = tune_batch("cmem", batch_size=8, repeats=args.repeats, sizes=[(288, 168)], samples=[880],
-                        segs=(1, 2, 4))
-        write_table(plain, tri, near, cm, args.out)
+        cm = tune_batch_cmem(repeats=args.repeats)
+        write_table(plain, plain_cmem, tri, near, cm, args.out)
         print("wrote", args.out)
 
 
