@@ -838,10 +838,10 @@ __device__ __forceinline__ void render_tile(const RequestDev& R, int tx, int ty,
     if (!certain && valid) {
       int s = 0, e = N;
       bool used64 = false;
-      // the float-float tier pays off in the records and pairs trilinear
-      // kernels (pairs: 8.75 -> 8.57 ms on 64 orbit renders); in the others
-      // its registers cost more than the FP64 searches it saves
-      if constexpr (INTERP == TRILINEAR && (AXES == AXES_DDA || AXES == AXES_DDA_PAIRS)) {
+      // the float-float tier pays off in the trilinear kernels (on 64 orbit
+      // renders: pairs 8.75 -> 8.57 ms, compact 10.33 -> 10.12 ms); in the
+      // nearest ones its registers cost more than the FP64 searches it saves
+      if constexpr (INTERP == TRILINEAR) {
         // An axis the FP32 bound leaves undecided is decided in float-float:
         // its interval ends are the first samples past the box's first and
         // last planes, u = P / (d dt) - K as in the nearest walk, with that
