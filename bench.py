@@ -34,9 +34,10 @@ over all 512 requests.
              served images
 
 `--impl reference` times only the CPU implementation (bounded samples).
-`--workload c3|c4` runs one of the extra blocks alone; `--profile-case
-trilinear|nearest|compact|cmem` runs a small fixed batch to profile one
-kernel class. Multi-GPU (torchrun): replicas, one per rank, barrier + max
+`--workload c3|c4` runs one of the extra blocks alone (`--c4-layout`,
+`--c4-promote-layout`, `--c4-promote-gb`, `--c4-uploaders` vary the config-4
+server); `--profile-case trilinear|nearest|compact|pairs|cmem` runs a small
+fixed batch to profile one kernel class. Multi-GPU (torchrun): replicas, one per rank, barrier + max
 over ranks (the c3/c4 blocks run at N = 1 only).
 """
 from __future__ import annotations
