@@ -450,7 +450,7 @@ birp_status birp_server_create(const birp_server_config* cfg, birp_server** out)
       c.cube_budget_bytes < 0 || !(c.max_wait_ms >= 0) ||
       (c.cube_layout != BIRP_CUBE_RECORDS && c.cube_layout != BIRP_CUBE_COMPACT && c.cube_layout != BIRP_CUBE_PAIRS) ||
       c.promoted_budget_bytes < 0 || c.promoted_budget_bytes > c.cube_budget_bytes || c.uploaders < 1 ||
-      c.uploaders > 8 ||
+      c.uploaders > 8 || (c.promoted_layout != BIRP_CUBE_RECORDS && c.promoted_layout != BIRP_CUBE_PAIRS) ||
       (c.promoted_budget_bytes > 0 &&
        !(c.promoted_layout == BIRP_CUBE_RECORDS ? c.cube_layout != BIRP_CUBE_RECORDS
          : c.promoted_layout == BIRP_CUBE_PAIRS  ? c.cube_layout == BIRP_CUBE_COMPACT

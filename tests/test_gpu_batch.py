@@ -198,7 +198,8 @@ def test_server_rejects_bad_promotion(birp):
     """A promoted layout must be faster than the server's own: records over
     compact or pairs, pairs over compact."""
     for base, promoted in [(birp.CUBE_RECORDS, birp.CUBE_RECORDS), (birp.CUBE_RECORDS, birp.CUBE_PAIRS),
-                           (birp.CUBE_PAIRS, birp.CUBE_PAIRS), (birp.CUBE_COMPACT, birp.CUBE_COMPACT)]:
+                           (birp.CUBE_PAIRS, birp.CUBE_PAIRS), (birp.CUBE_COMPACT, birp.CUBE_COMPACT),
+                           (birp.CUBE_COMPACT, 7)]:
         with pytest.raises(birp.BirpError):
             birp.Server(birp.server_config(cube_layout=base, promoted_layout=promoted, promoted_budget_bytes=1 << 30))
 
